@@ -1,0 +1,563 @@
+"""Benchmark of the GB300 device backend on the memory-bound strided workload.
+
+Workload (one "step"): for f64, f32 and i32 tensors of shape [32,64,128,128]
+in four input layouts (C-contiguous, F-contiguous, axis-permuted view,
+step-2 innermost slice), run the four hot-path operations of the rstsr
+tensor layer through the C ABI:
+  1. permute_dims(0,2,1,3) + to_contig (C order)   assign_arbitrary
+  2. a * b + c with c of shape [1,64,1,128]         fused one-pass kernel
+  3. sum over axes (1, 3)                           reduce_axes
+  4. argmax over the last axis                      argreduce_axes
+Inputs are seeded synthetic data (uniform(-1,1), i32 uniform in [-1000,1000])
+resident in HBM; every tensor is larger than the 129 MB L2 on its own.
+
+Metric: algorithmic HBM GB/s over the whole step (bytes the operations must
+move, counted per element of the logical tensors), the device-timed `value`;
+`e2e` repeats the step with the inputs copied from pinned host memory and the
+results copied back inside the timed region.
+
+`--impl reference` times the reference's CPU algorithm (the OpenMP
+restatement of rstsr's rayon kernels in oracle/) on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SHAPE = (32, 64, 128, 128)
+CSHAPE = (1, 64, 1, 128)
+N = int(np.prod(SHAPE))
+DTYPES = [("f64", np.float64), ("f32", np.float32), ("i32", np.int32)]
+LAYOUTS = ["c", "f", "perm", "slice"]
+METRIC = "f64 GEMM TFLOP/s Ozaki-split vs native FP64 at ≤1e-12 rel err; elementwise HBM GB/s"
+
+
+def c_stride(shape):
+    st, acc = [], 1
+    for d in reversed(shape):
+        st.append(acc)
+        acc *= max(d, 1)
+    return tuple(reversed(st))
+
+
+def f_stride(shape):
+    st, acc = [], 1
+    for d in shape:
+        st.append(acc)
+        acc *= max(d, 1)
+    return tuple(st)
+
+
+def layout_of(kind, shape):
+    """(base buffer length, view strides, offset) of one input layout."""
+    n = int(np.prod(shape))
+    if kind == "c":
+        return n, c_stride(shape), 0
+    if kind == "f":
+        return n, f_stride(shape), 0
+    if kind == "perm":
+        base = (shape[0], shape[2], shape[1], shape[3])
+        st = list(c_stride(base))
+        st[1], st[2] = st[2], st[1]
+        return n, tuple(st), 0
+    if kind == "slice":
+        base = tuple(shape[:-1]) + (shape[-1] * 2,)
+        st = list(c_stride(base))
+        st[-1] *= 2
+        return 2 * n, tuple(st), 0
+    raise ValueError(kind)
+
+
+def host_data(dt, n, seed):
+    rng = np.random.default_rng(seed)
+    if np.dtype(dt).kind == "f":
+        return rng.uniform(-1.0, 1.0, n).astype(dt)
+    return rng.integers(-1000, 1001, n).astype(dt)
+
+
+def permuted_view(shape, stride):
+    ax = (0, 2, 1, 3)
+    return tuple(shape[a] for a in ax), tuple(stride[a] for a in ax)
+
+
+def op_bytes(esize, kind):
+    """Algorithmic bytes of each operation (logical elements only)."""
+    copy_needed = kind != "perm"  # the permuted view of 'perm' is already C-contiguous
+    nout_sum = SHAPE[0] * SHAPE[2]
+    nout_arg = SHAPE[0] * SHAPE[1] * SHAPE[2]
+    return {
+        "to_contig": 2 * N * esize if copy_needed else 0,
+        "fma": (3 * N + int(np.prod(CSHAPE))) * esize,
+        "sum": (N + nout_sum) * esize,
+        "argmax": N * esize + nout_arg * 8,
+    }
+
+
+# ------------------------------------------------------------------ clocks
+
+
+class ClockSampler:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={dev}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        try:
+            rows = [l.split(",") for l in Path(self.path).read_text().strip().splitlines() if l.strip()]
+        except Exception:
+            return out
+        sm = [float(r[1]) for r in rows if len(r) > 8 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 8 and r[2].strip().replace(".", "").isdigit()]
+        if sm:
+            out["sm_mhz"] = float(np.median(sm))
+            out["sm_max_mhz"] = max(mx) if mx else None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            if len(r) > 8:
+                for i, nm in enumerate(names):
+                    if "Active" in r[5 + i] and "Not" not in r[5 + i]:
+                        reasons.add(nm)
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(rows)
+        return out
+
+
+# --------------------------------------------------------- GPU workload
+
+
+class Workload:
+    """Device buffers of one step and the calls that run it."""
+
+    def __init__(self, dev, lib, seed=0):
+        import rstsr_gb300 as rt
+        from rstsr_gb300._lib import Layout, dtype_code
+
+        self.dev, self.lib, self.rt = dev, lib, rt
+        self.cases = []
+        self.Layout = Layout
+        for di, (dname, dt) in enumerate(DTYPES):
+            code = dtype_code(dt)
+            esize = np.dtype(dt).itemsize
+            cbuf = host_data(dt, int(np.prod(CSHAPE)), seed + 100 + di)
+            c_t = rt.asarray(cbuf.reshape(CSHAPE), dev)
+            for li, kind in enumerate(LAYOUTS):
+                blen, stride, off = layout_of(kind, SHAPE)
+                ha = host_data(dt, blen, seed + 10 * di + li)
+                hb = host_data(dt, blen, seed + 1000 + 10 * di + li)
+                a = rt.from_host_layout(ha, SHAPE, stride, off, dev)
+                b = rt.from_host_layout(hb, SHAPE, stride, off, dev)
+                pshape, pstride = permuted_view(SHAPE, stride)
+                la_perm = Layout.make(pshape, pstride, off)
+                out_perm = rt.empty(pshape, code, dev, order="C")
+                # fused a*b+c: the output layout of `&a * &b`
+                d_t = rt.fma(a, b, c_t)
+                lab = d_t.layout()
+                lc_b = c_t.broadcast_to(SHAPE).layout()
+                sum_out = rt.empty((SHAPE[0], SHAPE[2]), code, dev, order="K", like=a.i((slice(None), 0, slice(None), 0)))
+                arg_out = rt.empty(SHAPE[:3], np.uint64, dev, order="K", like=a.i((slice(None), slice(None), slice(None), 0)))
+                self.cases.append(dict(
+                    dname=dname, kind=kind, code=code, esize=esize, a=a, b=b, c=c_t, d=d_t, la=a.layout(),
+                    lb=b.layout(), lab=lab, lcb=lc_b, la_perm=la_perm, out_perm=out_perm,
+                    copy=(kind != "perm"), sum_out=sum_out, arg_out=arg_out, ha=ha, hb=hb, hc=cbuf,
+                    bytes=op_bytes(esize, kind),
+                ))
+        self.ax_sum = (C.c_int64 * 2)(1, 3)
+        self.ax_arg = (C.c_int64 * 1)(3)
+
+    def total_bytes(self):
+        return sum(sum(c["bytes"].values()) for c in self.cases)
+
+    def run_op(self, c, op):
+        L, ctx = self.lib, self.dev.ctx
+        if op == "to_contig":
+            if c["copy"]:
+                rc = L.rstsr_cuda_assign_arbitrary(ctx, C.c_void_p(c["out_perm"].ptr), C.byref(c["out_perm"].layout()),
+                                                   c["code"], C.c_void_p(c["a"].ptr), C.byref(c["la_perm"]), c["code"], 0)
+            else:
+                rc = 0
+        elif op == "fma":
+            rc = L.rstsr_cuda_fma(ctx, c["code"], C.c_void_p(c["d"].ptr), C.byref(c["lab"]), C.c_void_p(c["a"].ptr),
+                                  C.byref(c["la"]), C.c_void_p(c["b"].ptr), C.byref(c["lb"]), C.c_void_p(c["c"].ptr),
+                                  C.byref(c["lcb"]))
+        elif op == "sum":
+            rc = L.rstsr_cuda_reduce_axes_into(ctx, 0, c["code"], C.c_void_p(c["a"].ptr), C.byref(c["la"]), self.ax_sum, 2,
+                                               C.c_void_p(c["sum_out"].ptr), C.byref(c["sum_out"].layout()))
+        else:
+            rc = L.rstsr_cuda_argreduce_axes_into(ctx, 1, c["code"], C.c_void_p(c["a"].ptr), C.byref(c["la"]),
+                                                  self.ax_arg, 1, C.c_void_p(c["arg_out"].ptr),
+                                                  C.byref(c["arg_out"].layout()))
+        if rc != 0:
+            raise RuntimeError(L.rstsr_cuda_last_error().decode())
+
+    def step(self):
+        for c in self.cases:
+            for op in ("to_contig", "fma", "sum", "argmax"):
+                self.run_op(c, op)
+
+
+def run_gpu(args):
+    import torch
+
+    import rstsr_gb300 as rt
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    lib = rt.lib()
+    dev = rt.DeviceCuda(local)
+    stream = torch.cuda.current_stream()
+    dev.set_stream(stream.cuda_stream)
+    wl = Workload(dev, lib, seed=0)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        wl.step()
+    barrier()
+    l0 = dev.launch_count()
+    clocks = ClockSampler(str(ROOT / "gpurun_out" / f"clocks_r{rank}.csv")) if rank == 0 else None
+    (ROOT / "gpurun_out").mkdir(exist_ok=True)
+    if clocks:
+        clocks.__enter__()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        wl.step()
+    ev1.record(stream)
+    barrier()
+    if clocks:
+        clocks.__exit__()
+    launches = dev.launch_count() - l0
+    t_ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([t_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(t.item())
+    step_bytes = wl.total_bytes()
+    value = step_bytes * world / (t_ms * 1e-3) / 1e9
+
+    # per-operation timing (dominant kernel for the roofline), same stream
+    per_op = {}
+    for op in ("to_contig", "fma", "sum", "argmax"):
+        reps = 3
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = dev.launch_count()
+        e0.record(stream)
+        for _ in range(reps):
+            for c in wl.cases:
+                wl.run_op(c, op)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        by = sum(c["bytes"][op] for c in wl.cases)
+        per_op[op] = dict(ms=round(ms, 4), gbs=round(by / (ms * 1e-3) / 1e9, 1), bytes=by,
+                          launches=(dev.launch_count() - n0) // reps)
+    # f64 C-contiguous fma alone: the single dominant kernel
+    dom = next(c for c in wl.cases if c["dname"] == "f64" and c["kind"] == "c")
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record(stream)
+    for _ in range(reps):
+        wl.run_op(dom, "fma")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fma_ms = e0.elapsed_time(e1) / reps
+    fma_bytes = dom["bytes"]["fma"]
+
+    e2e = run_e2e(wl, dev, stream, args, world) if not args.no_e2e else None
+    result = None
+    if rank == 0:
+        peaks = {}
+        try:
+            peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        except Exception:
+            pass
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = fma_bytes / (fma_ms * 1e-3) / 1e9
+        traffic = None
+        tpath = ROOT / "profiles" / "traffic.json"
+        if tpath.exists():
+            try:
+                traffic = json.loads(tpath.read_text()).get("fma_f64_c")
+            except Exception:
+                traffic = None
+        result = {
+            "metric": METRIC,
+            "value": round(value, 1),
+            "unit": "GB/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": round(t_ms, 4),
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64,f32,i32",
+            "data": "synthetic (seeded uniform; i32 uniform in [-1000,1000])",
+            "config": {
+                "workload": "strided ops [32,64,128,128] x {f64,f32,i32} x {C,F,permuted,step-2 slice}: "
+                            "permute(0,2,1,3)+to_contig, a*b+c (c [1,64,1,128]), sum(1,3), argmax(-1)",
+                "l2": "inputs larger than L2 (>=128 MiB per tensor), no flush",
+                "parallelism": f"replicas x{world}",
+                "step_bytes": step_bytes,
+            },
+            "roofline": {
+                "kernel": "fma (a*b+c, f64, C-contiguous, broadcast c)",
+                "bound": "hbm",
+                "achieved": round(achieved, 1),
+                "peak": peak,
+                "unit": "GB/s",
+                "frac": round(achieved / peak, 3),
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
+                "traffic": traffic,
+                "algorithmic_bytes_per_launch": fma_bytes,
+                "avg_launch_ms": round(fma_ms, 4),
+            },
+            "per_op": per_op,
+            "gpu_launches": int(launches),
+            "e2e": e2e,
+            "clocks": clocks.summary() if clocks else None,
+        }
+        if not args.no_cpu:
+            result["cpu_baseline"] = cpu_baseline(args)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return result
+
+
+def run_e2e(wl, dev, stream, args, world):
+    """Same step with host buffers: every input copied in (pinned host memory)
+    and every result copied out inside the timed region, through the C ABI."""
+    import torch
+
+    lib = wl.lib
+    pinned = []
+    for c in wl.cases:
+        ha = torch.from_numpy(c["ha"]).pin_memory()
+        hb = torch.from_numpy(c["hb"]).pin_memory()
+        hc = torch.from_numpy(np.ascontiguousarray(c["hc"])).pin_memory()
+        outs = dict(
+            perm=torch.empty(c["out_perm"].size * c["esize"], dtype=torch.uint8).pin_memory(),
+            d=torch.empty(wl_bytes(c["d"]), dtype=torch.uint8).pin_memory(),
+            s=torch.empty(wl_bytes(c["sum_out"]), dtype=torch.uint8).pin_memory(),
+            g=torch.empty(wl_bytes(c["arg_out"]), dtype=torch.uint8).pin_memory(),
+        )
+        pinned.append((ha, hb, hc, outs))
+
+    def step():
+        h2d = d2h = 0
+        for c, (ha, hb, hc, outs) in zip(wl.cases, pinned):
+            for host, t in ((ha, c["a"]), (hb, c["b"]), (hc, c["c"])):
+                nb = host.numel() * host.element_size()
+                rc = lib.rstsr_cuda_memcpy_h2d(dev.ctx, C.c_void_p(t.ptr), C.c_void_p(host.data_ptr()), C.c_size_t(nb))
+                assert rc == 0
+                h2d += nb
+            for op in ("to_contig", "fma", "sum", "argmax"):
+                wl.run_op(c, op)
+            for key, t in (("perm", c["out_perm"] if c["copy"] else None), ("d", c["d"]), ("s", c["sum_out"]),
+                           ("g", c["arg_out"])):
+                if t is None:
+                    continue
+                nb = outs[key].numel()
+                # asynchronous device->host copy on the context stream
+                rc = lib.rstsr_cuda_memcpy_d2d(dev.ctx, C.c_void_p(outs[key].data_ptr()), C.c_void_p(t.ptr),
+                                               C.c_size_t(nb))
+                assert rc == 0
+                d2h += nb
+        return h2d, d2h
+
+    for _ in range(max(1, args.warmup // 2)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        h2d, d2h = step()
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / steps
+    if world > 1:
+        tt = torch.tensor([t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    return {"value": round(wl.total_bytes() * world / t / 1e9, 1), "unit": "GB/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 3)}
+
+
+def wl_bytes(t):
+    lo, hi = t.offset, t.offset + 1
+    for d, s in zip(t.shape, t.stride):
+        if s > 0:
+            hi += s * (d - 1)
+        else:
+            lo += s * (d - 1)
+    return (hi - lo) * t.itemsize
+
+
+# ------------------------------------------------------------ CPU legs
+
+
+def cpu_sample_step(batch, nthreads, seed=0):
+    """One bounded sample of the step on the CPU oracle (OpenMP restatement of
+    the reference's rayon kernels): the first `batch` of the 32 leading
+    indices, all dtypes and layouts. Returns (seconds, algorithmic bytes)."""
+    from oracle import oracle as O
+
+    shape = (batch,) + SHAPE[1:]
+    n = int(np.prod(shape))
+    tot_t, tot_b = 0.0, 0
+    for di, (dname, dt) in enumerate(DTYPES):
+        esize = np.dtype(dt).itemsize
+        cbuf = host_data(dt, int(np.prod(CSHAPE)), seed + 100 + di)
+        for li, kind in enumerate(LAYOUTS):
+            blen, stride, off = layout_of(kind, shape)
+            a = O.Strided(host_data(dt, blen, seed + 10 * di + li), shape, stride, off)
+            b = O.Strided(host_data(dt, blen, seed + 1000 + 10 * di + li), shape, stride, off)
+            cst = O.Strided(cbuf, shape, (0, CSHAPE[3], 0, 1), 0)
+            pshape, pstride = permuted_view(shape, stride)
+            t0 = time.perf_counter()
+            if kind != "perm":
+                dst = O.empty_strided(pshape, c_stride(pshape), dt)
+                O.assign_arbitrary(dst, O.Strided(a.buf, pshape, pstride, off), 0, nthreads)
+            # the reference's two passes: tmp = a*b in the binary-op layout, tmp += c
+            from oracle import layout as OL
+
+            lab = OL.layout_for_binary_op((shape, stride, off), (shape, stride, off))
+            tmp = O.empty_strided(lab[0], lab[1], dt)
+            O.binary("mul", tmp, a, b, nthreads)
+            O.binary("add", tmp, tmp, cst, nthreads)
+            osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [1, 3])
+            so = O.empty_strided(osh, ost, dt)
+            O.reduce_axes("sum", a, [1, 3], so, nthreads)
+            osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [3])
+            go = O.empty_strided(osh, ost, np.uint64)
+            O.argreduce_axes(True, a, [3], go, nthreads)
+            tot_t += time.perf_counter() - t0
+            nb = op_bytes_n(esize, kind, n, shape)
+            tot_b += nb
+    return tot_t, tot_b
+
+
+def op_bytes_n(esize, kind, n, shape):
+    copy = 2 * n * esize if kind != "perm" else 0
+    return (copy + (3 * n + int(np.prod(CSHAPE))) * esize + (n + shape[0] * shape[2]) * esize
+            + n * esize + shape[0] * shape[1] * shape[2] * 8)
+
+
+def cpu_baseline(args):
+    from oracle import oracle as O
+
+    nth = O.max_threads()
+    batch = args.cpu_batch
+    t, b = cpu_sample_step(batch, nth)
+    return {"value": round(b / t / 1e9, 2), "unit": "GB/s", "cores": nth, "kind": "port",
+            "sample": f"one step at leading extent {batch} of 32 (all dtypes and layouts), {b / 1e9:.2f} GB in {t:.2f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+
+    nth = O.max_threads()
+    batch = args.cpu_batch
+    for _ in range(args.warmup):
+        cpu_sample_step(batch, nth)
+    tt, bb = 0.0, 0
+    for _ in range(args.steps):
+        t, b = cpu_sample_step(batch, nth)
+        tt += t
+        bb += b
+    value = bb / tt / 1e9
+    sample = f"each step: leading extent {batch} of 32, all dtypes and layouts ({bb / args.steps / 1e9:.2f} GB)"
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "GB/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(tt / args.steps * 1e3, 2),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64,f32,i32",
+        "data": "synthetic (seeded uniform; i32 uniform in [-1000,1000])",
+        "config": {"workload": "strided ops [32,64,128,128] x {f64,f32,i32} x {C,F,permuted,step-2 slice}: "
+                               "permute(0,2,1,3)+to_contig, a*b+c (c [1,64,1,128]), sum(1,3), argmax(-1)",
+                   "parallelism": "host cores"},
+        "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": nth, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-batch", type=int, default=4)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        res = run_reference(args)
+    else:
+        res = run_gpu(args)
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

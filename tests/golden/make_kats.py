@@ -1,0 +1,184 @@
+"""Writes reference_kats.json: known-answer cases transcribed from the
+reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
+
+Each case names the file:line it comes from. Integer literals in the
+reference's `tensor_from_nested!` are i32; `arange` defaults to i32 for integer
+ranges in these tests. Run:  python tests/golden/make_kats.py
+"""
+
+import json
+from pathlib import Path
+
+B3 = [[3, 6, 9], [4, 10, 5], [8, 3, 2]]
+A23 = [[1.0, 2.0, 3.0], [4.0, 5.0, 6.0]]
+P34 = [[1, 2, 3, 4], [5, 6, 7, 9], [10, 3, 4, 5]]
+CN = [[0, 1, 7, 0, 0], [3, 0, 0, 2, 19]]
+
+CASES = [
+    # ----------------------------------------------------------- argmax / argmin
+    *[
+        dict(src="rstsr-core/tests/core_func/reduction/test_argmax.rs:24-38", op="argmax_all", dtype="i32", a=a, expect=e)
+        for a, e in [
+            ([1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0], 0),
+            ([3, 3, 3, 3, 2, 2, 2, 2], 0),
+            ([0, 1, 2, 3, 4, 5, 6, 7], 7),
+            ([7, 6, 5, 4, 3, 2, 1, 0], 0),
+        ]
+    ],
+    dict(src="rstsr-core/tests/core_func/reduction/test_argmax.rs:72-78", op="argmax_axes", dtype="i32", a=B3, axes=[0],
+         expect=[2, 1, 0]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_argmax.rs:72-78", op="argmax_axes", dtype="i32", a=B3, axes=[1],
+         expect=[2, 1, 0]),
+    *[
+        dict(src="rstsr-core/tests/core_func/reduction/test_argmin.rs:20-34", op="argmin_all", dtype="i32", a=a, expect=e)
+        for a, e in [
+            ([1, 1, 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0], 8),
+            ([3, 3, 3, 3, 2, 2, 2, 2], 4),
+            ([0, 1, 2, 3, 4, 5, 6, 7], 0),
+            ([7, 6, 5, 4, 3, 2, 1, 0], 7),
+        ]
+    ],
+    dict(src="rstsr-core/tests/core_func/reduction/test_argmin.rs:46-52", op="argmin_axes", dtype="i32", a=B3, axes=[1],
+         expect=[0, 0, 2]),
+    # ----------------------------------------------------------------- sums
+    dict(src="rstsr-core/tests/core_func/reduction/test_sum.rs:24-33", op="sum_axes", dtype="i32",
+         a=[[1, 2, 3], [4, 5, 6], [7, 8, 9]], axes=[1], expect=[6, 15, 24]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_sum.rs:44-50", op="sum_all", dtype="i32",
+         a=[[1, 2, 3], [4, 5, 6], [7, 8, 9]], expect=45),
+    dict(src="rstsr-core/tests/core_func/reduction/test_sum.rs:52-62", op="sum_axes", dtype="i32",
+         a=list(range(24)), shape=[2, 3, 4], axes=[-2, -1], expect=[66, 210]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_sum.rs:64-73", op="sum_all", dtype="i32",
+         a=[[1, 2, 3], [4, 5, 6]], expect=21),
+    # ------------------------------------------------------------ mean/var/std
+    dict(src="rstsr-core/tests/core_func/reduction/test_mean.rs:19-30", op="mean_all", dtype="f64", a=A23, expect=3.5),
+    dict(src="rstsr-core/tests/core_func/reduction/test_mean.rs:19-30", op="mean_axes", dtype="f64", a=A23, axes=[0],
+         expect=[2.5, 3.5, 4.5]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_mean.rs:19-30", op="mean_axes", dtype="f64", a=A23, axes=[1],
+         expect=[2.0, 5.0]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_var.rs:20-33", op="var_all", dtype="f64", a=A23,
+         expect=2.9166666666666665),
+    dict(src="rstsr-core/tests/core_func/reduction/test_var.rs:20-33", op="var_axes", dtype="f64", a=A23, axes=[0],
+         expect=[2.25, 2.25, 2.25]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_var.rs:20-33", op="var_axes", dtype="f64", a=A23, axes=[1],
+         expect=[0.6666666666666666, 0.6666666666666666]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_std.rs:20-33", op="std_all", dtype="f64", a=A23,
+         expect=1.707825127659933),
+    dict(src="rstsr-core/tests/core_func/reduction/test_std.rs:20-33", op="std_axes", dtype="f64", a=A23, axes=[0],
+         expect=[1.5, 1.5, 1.5]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_std.rs:20-33", op="std_axes", dtype="f64", a=A23, axes=[1],
+         expect=[0.816496580927726, 0.816496580927726]),
+    # ------------------------------------------------------------- min / max
+    dict(src="rstsr-core/tests/core_func/reduction/test_max.rs:18-32", op="max_all", dtype="f64",
+         a=[3.0, 4.0, 5.0, 10.0, -3.0, -5.0, 6.0], expect=10.0),
+    dict(src="rstsr-core/tests/core_func/reduction/test_max.rs:18-32", op="max_axes", dtype="f64",
+         a=[[3.0, 6.0, 9.0], [4.0, 10.0, 5.0], [8.0, 3.0, 2.0]], axes=[0], expect=[8.0, 10.0, 9.0]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_max.rs:18-32", op="max_axes", dtype="f64",
+         a=[[3.0, 6.0, 9.0], [4.0, 10.0, 5.0], [8.0, 3.0, 2.0]], axes=[1], expect=[9.0, 10.0, 8.0]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_min.rs:18-32", op="min_all", dtype="f64",
+         a=[3.0, 4.0, 5.0, 10.0, -3.0, -5.0, 6.0], expect=-5.0),
+    dict(src="rstsr-core/tests/core_func/reduction/test_min.rs:18-32", op="min_axes", dtype="f64",
+         a=[[3.0, 6.0, 9.0], [4.0, 10.0, 5.0], [8.0, 3.0, 2.0]], axes=[0], expect=[3.0, 3.0, 2.0]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_min.rs:18-32", op="min_axes", dtype="f64",
+         a=[[3.0, 6.0, 9.0], [4.0, 10.0, 5.0], [8.0, 3.0, 2.0]], axes=[1], expect=[3.0, 4.0, 2.0]),
+    # ------------------------------------------------------------------ prod
+    dict(src="rstsr-core/tests/core_func/reduction/test_prod.rs:18-28", op="prod_axes", dtype="i32", a=P34, axes=[-1],
+         expect=[24, 1890, 600]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_prod.rs:31-46", op="prod_all", dtype="i32",
+         a=[1, 2, 10, 11, 6, 5, 4], expect=26400),
+    dict(src="rstsr-core/tests/core_func/reduction/test_prod.rs:31-46", op="prod_axes", dtype="i32", a=P34, axes=[0],
+         expect=[50, 36, 84, 180]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_prod.rs:55-63", op="prod_all", dtype="i32",
+         a=[[1, 2, 3], [4, 5, 6]], expect=720),
+    # ------------------------------------------------------------- all / any
+    dict(src="rstsr-core/tests/core_func/reduction/test_all.rs:19-34", op="all_all", dtype="bool",
+         a=[False, True, True, False], expect=False),
+    dict(src="rstsr-core/tests/core_func/reduction/test_all.rs:19-34", op="all_all", dtype="bool",
+         a=[True, True, True, True], expect=True),
+    dict(src="rstsr-core/tests/core_func/reduction/test_all.rs:19-34", op="all_all", dtype="bool",
+         a=[False, False, False, False], expect=False),
+    dict(src="rstsr-core/tests/core_func/reduction/test_all.rs:38-50", op="all_axes", dtype="bool",
+         a=[[False, False, True], [False, True, True], [True, True, True]], axes=[0], expect=[False, False, True]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_all.rs:38-50", op="all_axes", dtype="bool",
+         a=[[False, False, True], [False, True, True], [True, True, True]], axes=[1], expect=[False, False, True]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_any.rs:19-31", op="any_all", dtype="bool",
+         a=[False, False, True, False], expect=True),
+    dict(src="rstsr-core/tests/core_func/reduction/test_any.rs:19-31", op="any_all", dtype="bool",
+         a=[False, False, False, False], expect=False),
+    dict(src="rstsr-core/tests/core_func/reduction/test_any.rs:35-47", op="any_axes", dtype="bool",
+         a=[[False, False, False], [False, True, False], [True, True, False]], axes=[0], expect=[True, True, False]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_any.rs:35-47", op="any_axes", dtype="bool",
+         a=[[False, False, False], [False, True, False], [True, True, False]], axes=[1], expect=[False, True, True]),
+    # --------------------------------------------------------- count_nonzero
+    dict(src="rstsr-core/tests/core_func/reduction/test_count_nonzero.rs:18-28", op="count_nonzero_axes", dtype="i32",
+         a=CN, axes=[1], expect=[2, 3]),
+    dict(src="rstsr-core/tests/core_func/reduction/test_count_nonzero.rs:36-44", op="count_nonzero_all", dtype="i32",
+         a=CN, expect=5),
+    # ------------------------------------------------------------- to_contig
+    dict(src="rstsr-core/tests/core_func/manipulation/test_to_contig.rs:56-80", op="to_contig", dtype="i32",
+         a=list(range(12)), shape=[3, 4], view=dict(transpose=[1, 0]),
+         expect=[[0, 4, 8], [1, 5, 9], [2, 6, 10], [3, 7, 11]]),
+    dict(src="rstsr-core/tests/core_func/manipulation/test_to_contig.rs:82-101", op="to_contig", dtype="i32",
+         a=list(range(24)), shape=[4, 6], view=dict(slice=[[None, None, 2], [None, None, 2]]),
+         view_stride=[12, 2], expect=[[0, 2, 4], [12, 14, 16]]),
+    dict(src="rstsr-core/tests/core_func/manipulation/test_to_contig.rs:270-287", op="to_contig", dtype="i32",
+         a=list(range(12)), shape=[3, 4], view=dict(flip=0),
+         expect=[[8, 9, 10, 11], [4, 5, 6, 7], [0, 1, 2, 3]]),
+    # ------------------------------------------------------------ arithmetic
+    dict(src="rstsr-core/tests/core_func/operators/test_arithmetic.rs:14-22", op="add", dtype="i32",
+         a=[[1, 2], [3, 4]], b=[[10, 20], [30, 40]], expect=[[11, 22], [33, 44]]),
+    dict(src="rstsr-core/tests/core_func/operators/test_arithmetic.rs:24-31", op="add", dtype="i32",
+         a=[[1, 2, 3], [4, 5, 6]], b=[10, 20, 30], expect=[[11, 22, 33], [14, 25, 36]]),
+    dict(src="rstsr-core/tests/core_func/operators/test_arithmetic.rs:36-44", op="sub", dtype="i32",
+         a=[[10, 20], [30, 40]], b=[[1, 2], [3, 4]], expect=[[9, 18], [27, 36]]),
+    dict(src="rstsr-core/tests/core_func/operators/test_arithmetic.rs:49-57", op="mul", dtype="i32",
+         a=[[1, 2], [3, 4]], b=[10, 100], expect=[[10, 200], [30, 400]]),
+    dict(src="rstsr-core/tests/core_func/operators/test_arithmetic.rs:62-72", op="div", dtype="f64",
+         a=[[10.0, 20.0], [30.0, 40.0]], b=[[2.0, 4.0], [5.0, 8.0]], expect=[[5.0, 5.0], [6.0, 5.0]]),
+    dict(src="rstsr-core/tests/core_func/operators/test_arithmetic.rs:77-92", op="rem", dtype="i32",
+         a=[[10, 21], [33, 44]], b=[[3, 4], [5, 7]], expect=[[1, 1], [3, 2]]),
+    # ---------------------------------------------------------------- matmul
+    dict(src="rstsr-core/tests/core_func/operators/test_arithmetic.rs:77-92", op="matmul", dtype="i32",
+         a=[[10, 21], [33, 44]], b=[[3, 4], [5, 7]], expect=[[135, 187], [319, 440]]),
+    dict(src="rstsr-core/tests/core_func/linalg/test_matmul.rs:17-31", op="matmul", dtype="i32",
+         a=[1, 2], b=[[3], [4]], expect=[11]),
+    dict(src="rstsr-core/tests/core_func/linalg/test_matmul.rs:17-31", op="matmul", dtype="i32",
+         a=[[3], [4]], b=[[1, 2]], expect=[[3, 6], [4, 8]]),
+    dict(src="rstsr-core/tests/core_func/linalg/test_matmul.rs:34-43", op="matmul", dtype="i32",
+         a=[1, 2], b=[[1, 2], [3, 4]], expect=[7, 10]),
+    dict(src="rstsr-core/tests/core_func/linalg/test_matmul.rs:46-55", op="matmul", dtype="i32",
+         a=[[1, 2], [3, 4]], b=[1, 2], expect=[5, 11]),
+    dict(src="rstsr-core/tests/core_func/linalg/test_matmul.rs:58-70", op="matmul", dtype="i32",
+         a=[[1, 2], [3, 4]], b=[[1, 0], [1, 1]], expect=[[3, 2], [7, 4]]),
+    dict(src="rstsr-core/tests/core_func/linalg/test_matmul.rs:58-70", op="matmul", dtype="i32",
+         a=[[1, 0], [1, 1]], b=[[1, 2], [3, 4]], expect=[[1, 2], [4, 6]]),
+    dict(src="rstsr-core/tests/core_func/linalg/test_matmul.rs:75-90", op="matmul", dtype="i32",
+         a=[[[1, 2], [3, 4]], [[1, 0], [1, 1]]], b=[[1, 2], [3, 4]], expect=[[[7, 10], [15, 22]], [[1, 2], [4, 6]]]),
+    dict(src="rstsr-core/src/tensor/linalg/matmul.rs:366-374", op="matmul_from", dtype="f64",
+         a=[float(x) for x in range(15)], shape_a=[3, 5], b=[float(x) for x in range(20)], shape_b=[5, 4],
+         c=[float(x) for x in range(12)], shape_c=[3, 4], alpha=2.0, beta=1.5,
+         expect=[240.0, 261.5, 283.0, 304.5, 646.0, 717.5, 789.0, 860.5, 1052.0, 1173.5, 1295.0, 1416.5]),
+    dict(src="crates-device/rstsr-openblas/tests/test_workable.rs:14-27", op="batched_linspace_stats", dtype="f64",
+         n=1048576, shape=[16, 256, 256], a_range=[0.0, 1.0], b_range=[1.0, 2.0],
+         expect=dict(mean_all=213.2503660477036, std_all=148.88523481701804), tol=1e-6),
+    # ---------------------------------------------------------- layout algebra
+    dict(src="rstsr-common/src/layout/rearrangement.rs:466-496", op="greedy_layout", keep_shape=False,
+         shape=[5, 1, 2, 1, 3, 6], stride=[1000, 10, 10, 40, 0, 100],
+         expect=dict(shape=[2, 6, 5, 1, 1, 1], stride=[10, 100, 1000, 0, 0, 0])),
+    dict(src="rstsr-common/src/layout/rearrangement.rs:466-496", op="greedy_layout", keep_shape=True,
+         shape=[5, 1, 2, 1, 3, 6], stride=[1000, 10, 10, 40, 0, 100],
+         expect=dict(shape=[1, 1, 3, 2, 6, 5], stride=[10, 40, 0, 10, 100, 1000])),
+    dict(src="rstsr-common/src/layout/rearrangement.rs:466-496", op="greedy_layout", keep_shape=True,
+         shape=[2, 3, 4], stride=[12, 4, 1], expect=dict(shape=[4, 3, 2], stride=[1, 4, 12])),
+    dict(src="rstsr-common/src/layout/rearrangement.rs:466-496", op="greedy_layout", keep_shape=False,
+         shape=[2, 3, 4], stride=[1, 2, 6], expect=dict(shape=[2, 3, 4], stride=[1, 2, 6])),
+]
+
+
+def main() -> None:
+    out = Path(__file__).resolve().parent / "reference_kats.json"
+    out.write_text(json.dumps(CASES, indent=1) + "\n")
+    print(f"wrote {len(CASES)} cases to {out}")
+
+
+if __name__ == "__main__":
+    main()
