@@ -121,7 +121,7 @@ class ClockSampler:
             dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={dev}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
@@ -247,7 +247,10 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     lib = rt.lib()
     dev = rt.DeviceCuda(local)
-    stream = torch.cuda.current_stream()
+    # one explicit (non-default) stream carries every library launch and the
+    # timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     dev.set_stream(stream.cuda_stream)
     wl = Workload(dev, lib, seed=0)
     torch.cuda.synchronize()
@@ -265,6 +268,7 @@ def run_gpu(args):
     (ROOT / "gpurun_out").mkdir(exist_ok=True)
     if clocks:
         clocks.__enter__()
+        time.sleep(0.3)  # let the sampler start before the timed region
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for _ in range(args.steps):
@@ -544,7 +548,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")

@@ -97,7 +97,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         raise RuntimeError(f"compilation failed for: {', '.join(errors)}")
     newest = max(o.stat().st_mtime for o in objs)
     if not LIB.exists() or LIB.stat().st_mtime < newest:
-        link = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart", "-lcuda"]
+        link = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
         cmd, rc, out = _run(link)
         if rc != 0:
             print(out, file=sys.stderr)

@@ -24,6 +24,7 @@ struct rstsr_ctx {
     std::atomic<uint64_t> launches{0};
     bool capturing = false;
     uint64_t launches_at_capture = 0;
+    int* dev_err = nullptr;  // device word: non-zero after a kernel gave up a bounded wait
 };
 
 namespace rstsr {

@@ -177,6 +177,13 @@ int rstsr_cuda_ctx_create(int32_t device, rstsr_ctx** out) {
     // high rate and returning memory to the driver each time is slow.
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    e = cudaMalloc(&c->dev_err, 256);
+    if (e == cudaSuccess) e = cudaMemset(c->dev_err, 0, 256);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(c->own_stream);
+        delete c;
+        return cuda_fail(e, "error word allocation");
+    }
     *out = c;
     return RSTSR_OK;
 }
@@ -187,6 +194,7 @@ int rstsr_cuda_ctx_destroy(rstsr_ctx* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    if (ctx->dev_err) cudaFree(ctx->dev_err);
     delete ctx;
     return RSTSR_OK;
 }
@@ -196,6 +204,14 @@ int rstsr_cuda_ctx_sync(rstsr_ctx* ctx) {
     int s = enter(ctx);
     if (s) return s;
     RSTSR_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    // a kernel that gave up a bounded wait leaves its code in the error word
+    int code = 0;
+    RSTSR_CUDA_TRY(cudaMemcpy(&code, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (code != 0) {
+        cudaMemset(ctx->dev_err, 0, sizeof(int));
+        return fail(RSTSR_ERR_TIMEOUT, "a device-side wait timed out (code " + std::to_string(code) +
+                                           "); the results of the affected call are invalid");
+    }
     return RSTSR_OK;
 }
 
