@@ -305,6 +305,26 @@ int rstsr_cuda_argreduce_axes_into(rstsr_ctx* ctx, int32_t is_max, rstsr_dtype t
                                    const int64_t* axes, int32_t naxes,
                                    void* out, const rstsr_layout* lout);
 
+/* Allocation-free sum over axes. No counterpart in the reference: it exists
+ * for callers that must not have the library allocate device memory -- a
+ * host that hands out all GPU memory from its own arena, a latency-critical
+ * loop that cannot afford the synchronisation of cudaMalloc/cudaFree, or a
+ * plugin host that forbids allocations outside its own allocator. It takes a
+ * CUDA stream instead of a context (creating a context allocates) and the
+ * caller provides input and output, the output laid out over the kept axes
+ * (any strides). The split reduction's partial sums live in one fixed static
+ * device array of RSTSR_NOALLOC_SCRATCH_BYTES that every GPU loading this
+ * library holds until the process exits; a reduction that would need more
+ * scratch is rejected with RSTSR_ERR_VALUE_OUT_OF_RANGE. The first call on a
+ * device looks up that array's device address (cudaGetSymbolAddress), so make
+ * the first call on each device before any stream capture. All calls share
+ * the array: calls that can overlap on the GPU (different streams, or
+ * different host threads) race on it and must be serialised by the caller.
+ * Supported dtypes: f64, f32, i32, i64. Never calls cudaMalloc or cudaFree. */
+#define RSTSR_NOALLOC_SCRATCH_BYTES (1u << 20)
+int rstsr_cuda_sum_axes_noalloc(void* cuda_stream, rstsr_dtype ta, const void* a, const rstsr_layout* la,
+                                const int64_t* axes, int32_t naxes, void* out, const rstsr_layout* lout);
+
 /* ---------------------------------------------------------------- matmul */
 
 /* How a floating-point GEMM is evaluated on the tensor cores. */

@@ -166,6 +166,7 @@ _SIGS = {
     "rstsr_cuda_reduce_axes_layout": ([_L, C.POINTER(C.c_int64), _I, _L], C.c_int),
     "rstsr_cuda_reduce_axes": ([_P, _I, _I, _P, _L, C.POINTER(C.c_int64), _I, C.POINTER(_P), _L], C.c_int),
     "rstsr_cuda_reduce_axes_into": ([_P, _I, _I, _P, _L, C.POINTER(C.c_int64), _I, _P, _L], C.c_int),
+    "rstsr_cuda_sum_axes_noalloc": ([_P, _I, _P, _L, C.POINTER(C.c_int64), _I, _P, _L], C.c_int),
     "rstsr_cuda_argreduce_all": ([_P, _I, _I, _P, _L, C.POINTER(C.c_uint64)], C.c_int),
     "rstsr_cuda_argreduce_axes": ([_P, _I, _I, _P, _L, C.POINTER(C.c_int64), _I, C.POINTER(_P), _L], C.c_int),
     "rstsr_cuda_argreduce_axes_into": ([_P, _I, _I, _P, _L, C.POINTER(C.c_int64), _I, _P, _L], C.c_int),

@@ -157,17 +157,18 @@ static void build_red_space(const Layout& ls, RedSpace* r) {
     }
 }
 
-// Plan and launch a reduction of `a` (dtype t_in, layout La) over `axes`
-// into `out` (dtype t_kout, layout Lo with the kept shape).
-static int run_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, int kind, const void* a, const Layout& La,
-                      const int64_t* axes, int naxes, void* out, const Layout& Lo) {
+// Plan a reduction of `a` (dtype t_in, layout La) over `axes` into `out`
+// (layout Lo with the kept shape): fills every field of *pp except the
+// scratch pointer. Allocates nothing. pp->nout == 0 means nothing to do.
+int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const Layout& La, const int64_t* axes,
+                int naxes, void* out, const Layout& Lo, RedParams* pp) {
     Layout ls, lm;
     Error e;
     if (!split_axes(La, axes, naxes, &ls, &lm, nullptr, &e)) return fail(e.code, e.msg);
     if (lm.ndim != Lo.ndim || !std::equal(lm.shape, lm.shape + lm.ndim, Lo.shape))
         return fail(RSTSR_ERR_INVALID_LAYOUT, "reduction output shape does not match the kept axes (" +
                                                   Lo.repr() + " vs " + lm.repr() + ")");
-    RedParams p;
+    RedParams& p = *pp;
     memset(&p, 0, sizeof(p));
     p.nred = ls.size();
     p.nout = lm.size();
@@ -240,6 +241,16 @@ static int run_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, int kind, const 
         p.chunk = chunk;
         p.vec = 0;
     }
+    return RSTSR_OK;
+}
+
+// Plan and launch a reduction of `a` (dtype t_in, layout La) over `axes`
+// into `out` (dtype t_kout, layout Lo with the kept shape).
+static int run_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, int kind, const void* a, const Layout& La,
+                      const int64_t* axes, int naxes, void* out, const Layout& Lo) {
+    RedParams p;
+    int s = plan_reduce(ctx, op, t_in, a, La, axes, naxes, out, Lo, &p);
+    if (s || p.nout == 0) return s;
     return launch_kind(ctx, t_in, kind, p);
 }
 

@@ -1,0 +1,113 @@
+// An allocation-free variant of the axis-sum reduction.
+//
+// Some hosts cannot let a library allocate device memory: a caller that owns
+// every byte of GPU memory through its own arena (so a cudaMalloc behind its
+// back would fail or fragment the arena), a latency-critical loop where the
+// implicit synchronisation of cudaMalloc/cudaFree is not acceptable, or a
+// plugin host that forbids allocations outside its own allocator. The
+// regular rstsr_cuda_reduce_axes_into may take scratch memory from the
+// context's pool (the per-chunk partial sums of the split reduction) and
+// needs a context, whose creation allocates. rstsr_cuda_sum_axes_noalloc runs
+// the same kernels on a caller-supplied stream with its scratch in a fixed
+// static device array of RSTSR_NOALLOC_SCRATCH_BYTES; every GPU that loads
+// the library holds that array until the process exits.
+#include <mutex>
+
+#include "reduce_kernel.cuh"
+
+namespace rstsr {
+
+int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const Layout& La, const int64_t* axes,
+                int naxes, void* out, const Layout& Lo, RedParams* pp);
+
+// The scratch shared by every call of the allocation-free entry point.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[RSTSR_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+static void* g_scratch_addr[kMaxDevices];
+static std::mutex g_scratch_mutex;
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device (the host-side symbol is only a stand-in, not a device address).
+static int scratch_address(int device, void** out) {
+    if (device < 0 || device >= kMaxDevices) return fail(RSTSR_ERR_DEVICE, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_scratch_addr[device] = p;
+    }
+    *out = g_scratch_addr[device];
+    return RSTSR_OK;
+}
+
+template <typename T>
+static int launch_sum_noalloc(cudaStream_t stream, RedParams p, void* scratch) {
+    using Acc = typename Red<T, kRedSum>::Acc;
+    const int opc = kRedThreads >> p.glog;
+    const int64_t gx = (p.nout + opc - 1) / opc;
+    if (gx > INT32_MAX || p.nsplit > 65535) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "reduction too large");
+    if (p.nsplit > 1) {
+        const size_t need = (size_t)p.nsplit * (size_t)p.nout * sizeof(Acc);
+        if (need > RSTSR_NOALLOC_SCRATCH_BYTES)
+            return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE,
+                        "sum_axes_noalloc: this reduction needs " + std::to_string(need) +
+                            " bytes of scratch, more than the fixed " +
+                            std::to_string((size_t)RSTSR_NOALLOC_SCRATCH_BYTES) + " bytes");
+        // every partial is written by the first kernel before the second
+        // reads it, so the scratch needs no clearing
+        p.partial = scratch;
+    } else {
+        p.partial = nullptr;
+    }
+    reduce_kernel<T, kRedSum><<<dim3((unsigned)gx, (unsigned)p.nsplit), kRedThreads, 0, stream>>>(p);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "reduce_kernel");
+    if (p.nsplit > 1) {
+        const int64_t gc = (p.nout + kRedThreads - 1) / kRedThreads;
+        reduce_combine_kernel<T, kRedSum><<<(unsigned)gc, kRedThreads, 0, stream>>>(p);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "reduce_combine_kernel");
+    }
+    return RSTSR_OK;
+}
+
+}  // namespace rstsr
+
+using namespace rstsr;
+
+extern "C" int rstsr_cuda_sum_axes_noalloc(void* stream, rstsr_dtype ta, const void* a, const rstsr_layout* la,
+                                           const int64_t* axes, int32_t naxes, void* out,
+                                           const rstsr_layout* lout) {
+    clear_error();
+    if (ta != RSTSR_F64 && ta != RSTSR_F32 && ta != RSTSR_I32 && ta != RSTSR_I64)
+        return fail(RSTSR_ERR_UNIMPLEMENTED, "sum_axes_noalloc supports f64, f32, i32 and i64");
+    int s = check_layout(la, "a");
+    if (!s) s = check_layout(lout, "out");
+    if (s) return s;
+    if (naxes < 0 || (naxes > 0 && !axes)) return fail(RSTSR_ERR_INVALID_VALUE, "bad axes");
+    int device = -1;
+    RSTSR_CUDA_TRY(cudaGetDevice(&device));
+    void* scratch = nullptr;
+    s = scratch_address(device, &scratch);
+    if (s) return s;
+    // a context on the stack: the planner reads only the stream and the SM
+    // count from it, and nothing here allocates
+    rstsr_ctx local;
+    local.device = device;
+    local.stream = (cudaStream_t)stream;
+    RSTSR_CUDA_TRY(cudaDeviceGetAttribute(&local.num_sms, cudaDevAttrMultiProcessorCount, device));
+    const Layout La = Layout::from_abi(*la), Lo = Layout::from_abi(*lout);
+    if (Lo.size() > 0 && !out) return fail(RSTSR_ERR_INVALID_VALUE, "null output pointer");
+    if (La.size() > 0 && !a) return fail(RSTSR_ERR_INVALID_VALUE, "null input pointer");
+    RedParams p;
+    s = plan_reduce(&local, RSTSR_RED_SUM, ta, a, La, axes, naxes, out, Lo, &p);
+    if (s || p.nout == 0) return s;
+    switch (ta) {
+        case RSTSR_F64: return launch_sum_noalloc<double>(local.stream, p, scratch);
+        case RSTSR_F32: return launch_sum_noalloc<float>(local.stream, p, scratch);
+        case RSTSR_I32: return launch_sum_noalloc<int32_t>(local.stream, p, scratch);
+        default: return launch_sum_noalloc<int64_t>(local.stream, p, scratch);
+    }
+}
