@@ -164,7 +164,7 @@ class ClockSampler:
 class Workload:
     """Device buffers of one step and the calls that run it."""
 
-    def __init__(self, dev, lib, seed=0):
+    def __init__(self, dev, lib, seed=0, dtypes=None, layouts=None):
         import rstsr_gb300 as rt
         from rstsr_gb300._lib import Layout, dtype_code
 
@@ -172,11 +172,15 @@ class Workload:
         self.cases = []
         self.Layout = Layout
         for di, (dname, dt) in enumerate(DTYPES):
+            if dtypes and dname not in dtypes:
+                continue
             code = dtype_code(dt)
             esize = np.dtype(dt).itemsize
             cbuf = host_data(dt, int(np.prod(CSHAPE)), seed + 100 + di)
             c_t = rt.asarray(cbuf.reshape(CSHAPE), dev)
             for li, kind in enumerate(LAYOUTS):
+                if layouts and kind not in layouts:
+                    continue
                 blen, stride, off = layout_of(kind, SHAPE)
                 ha = host_data(dt, blen, seed + 10 * di + li)
                 hb = host_data(dt, blen, seed + 1000 + 10 * di + li)
@@ -252,7 +256,8 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     dev.set_stream(stream.cuda_stream)
-    wl = Workload(dev, lib, seed=0)
+    wl = Workload(dev, lib, seed=0, dtypes=args.dtypes.split(",") if args.dtypes else None,
+                  layouts=args.layouts.split(",") if args.layouts else None)
     torch.cuda.synchronize()
 
     def barrier():
@@ -303,8 +308,23 @@ def run_gpu(args):
         by = sum(c["bytes"][op] for c in wl.cases)
         per_op[op] = dict(ms=round(ms, 4), gbs=round(by / (ms * 1e-3) / 1e9, 1), bytes=by,
                           launches=(dev.launch_count() - n0) // reps)
+    # per (dtype, layout, op) GB/s
+    per_case = {}
+    for c in wl.cases:
+        for op in ("to_contig", "fma", "sum", "argmax"):
+            if c["bytes"][op] == 0:
+                continue
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(3):
+                wl.run_op(c, op)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / 3
+            per_case[f"{c['dname']}/{c['kind']}/{op}"] = round(c["bytes"][op] / (ms * 1e-3) / 1e9, 0)
     # f64 C-contiguous fma alone: the single dominant kernel
-    dom = next(c for c in wl.cases if c["dname"] == "f64" and c["kind"] == "c")
+    dom = next((c for c in wl.cases if c["dname"] == "f64" and c["kind"] == "c"), wl.cases[0])
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     reps = 10
@@ -366,16 +386,213 @@ def run_gpu(args):
                 "avg_launch_ms": round(fma_ms, 4),
             },
             "per_op": per_op,
+            "per_case": per_case,
             "gpu_launches": int(launches),
             "e2e": e2e,
             "clocks": clocks.summary() if clocks else None,
         }
+        if not args.no_gemm:
+            result["gemm"] = run_gemm_section(dev, stream)
+            result["gemm"].update(run_batched_section(dev, stream))
+            result["small_f64"] = run_small_section(dev, stream)
         if not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline(args)
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return result
+
+
+def _time_events(stream, fn, reps):
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps * 1e-3
+
+
+def run_gemm_section(dev, stream):
+    """The GEMM half of the metric: the f64 electronic-structure contraction
+    C = Bm^T Bm (Bm = B[P=1000, i=50, a=300] reshaped to 1000 x 15000, entries
+    N(0,1) exp(-0.01 P), seed 0) through the Ozaki split against native FP64
+    (cuBLAS DGEMM on the same GPU, also the FP64 oracle for the error), and the
+    f32 three-term bf16 split on 8192^3 and 65536x256x256 (entries
+    U(-1,1) 2^U(-8,8)) against cuBLAS SGEMM, errors against FP64."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    out = {}
+    rng = np.random.default_rng(0)
+    P, Q = 1000, 50 * 300
+    bm = rng.standard_normal((P, Q)) * np.exp(-0.01 * np.arange(P))[:, None]
+    t = rt.asarray(bm, dev)
+    c = rt.empty((Q, Q), np.float64, dev)
+    run = lambda: rt.matmul_into(c, t.t(), t, 1.0, 0.0)
+    sec = _time_events(stream, run, 3)
+    slices = int(rt.lib().rstsr_cuda_last_ozaki_slices())
+    flops = 2.0 * Q * Q * P
+    tb = torch.from_numpy(bm).cuda()
+    ref = tb.T @ tb
+    sec_ref = _time_events(stream, lambda: tb.T @ tb, 1)
+    got = torch.as_tensor(c.to_numpy()).cuda()
+    err = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
+    out["c3_ozaki_f64"] = {
+        "shape": "Bm^T Bm, m=n=15000, k=1000 (SYRK path)", "tflops": round(flops / sec / 1e12, 2),
+        "ms": round(sec * 1e3, 3), "slices": slices, "rel_err_frobenius": err,
+        "native_fp64_cublas_tflops": round(flops / sec_ref / 1e12, 3), "native_ms": round(sec_ref * 1e3, 2),
+        "speedup_vs_native_fp64": round(sec_ref / sec, 1), "flop_count": "2mnk (full product)",
+    }
+    del c, ref, got, tb
+    torch.cuda.empty_cache()
+    for name, (m, n, k) in (("c4_split_f32_8192", (8192, 8192, 8192)), ("c4_split_f32_tall", (65536, 256, 256))):
+        a = (rng.uniform(-1, 1, (m, k)) * 2.0 ** rng.uniform(-8, 8, (m, k))).astype(np.float32)
+        b = (rng.uniform(-1, 1, (k, n)) * 2.0 ** rng.uniform(-8, 8, (k, n))).astype(np.float32)
+        ta, tb2 = rt.asarray(a, dev), rt.asarray(b, dev)
+        c = rt.empty((m, n), np.float32, dev)
+        sec = _time_events(stream, lambda: rt.matmul_into(c, ta, tb2), 3)
+        fa, fb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+        ref = fa.double() @ fb.double()
+        torch.backends.cuda.matmul.allow_tf32 = False
+        sec_s = _time_events(stream, lambda: fa @ fb, 3)
+        sref = (fa @ fb).double()
+        got = torch.as_tensor(c.to_numpy()).cuda().double()
+        nr = torch.linalg.norm(ref)
+        out[name] = {
+            "shape": f"{m}x{n}x{k}", "tflops": round(2.0 * m * n * k / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
+            "rel_err_vs_fp64": (torch.linalg.norm(got - ref) / nr).item(),
+            "cublas_sgemm_tflops": round(2.0 * m * n * k / sec_s / 1e12, 2),
+            "cublas_sgemm_rel_err_vs_fp64": (torch.linalg.norm(sref - ref) / nr).item(),
+        }
+        del a, b, ta, tb2, c, fa, fb, ref, sref, got
+        torch.cuda.empty_cache()
+    return out
+
+
+def run_batched_section(dev, stream):
+    """Batched / grouped matmul and the graph-captured op chain:
+    (i) 512 f64 GEMMs with m, n, k uniform in [16, 512] (seed 0) as one grouped
+    launch; (ii) the broadcast batch [64,1,256,256] % [1,32,256,256] f64
+    (2048 products, matmul rule 7); (iii) matmul [256,256] % [256,256] ->
+    broadcast bias add [256] -> sum_axes(1), f64, captured once as a CUDA graph
+    and replayed 1000 times, against the same chain issued eagerly."""
+    import ctypes as C
+
+    import torch
+
+    import rstsr_gb300 as rt
+    from rstsr_gb300._lib import GemmProblem, call
+
+    out = {}
+    rng = np.random.default_rng(0)
+    # (i) uneven grouped
+    dims = rng.integers(16, 513, (512, 3))
+    probs, keep, flops = [], [], 0.0
+    for m, n, k in dims:
+        m, n, k = int(m), int(n), int(k)
+        a = rng.uniform(-1, 1, (m, k))
+        b = rng.uniform(-1, 1, (k, n))
+        ta, tb = rt.asarray(a, dev), rt.asarray(b, dev)
+        tc = rt.empty((m, n), np.float64, dev)
+        keep.append((a, b, ta, tb, tc))
+        probs.append(GemmProblem(m, n, k, k, n, n, ta.ptr, tb.ptr, tc.ptr, 1.0, 0.0))
+        flops += 2.0 * m * n * k
+    arr = (GemmProblem * len(probs))(*probs)
+    run = lambda: call("rstsr_cuda_gemm_grouped", dev.ctx, 0, arr, len(probs), None)
+    l0 = dev.launch_count()
+    run()
+    torch.cuda.synchronize()
+    launches = dev.launch_count() - l0
+    sec = _time_events(stream, run, 5)
+    num = den = 0.0
+    for a, b, _, _, tc in keep:
+        r = a @ b
+        num += float(np.sum((tc.to_numpy() - r) ** 2))
+        den += float(np.sum(r * r))
+    out["c5_grouped_f64_512"] = {"tflops": round(flops / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
+                                 "sum_2mnk": flops, "rel_err_frobenius": (num / den) ** 0.5,
+                                 "launches_per_call": int(launches)}
+    del keep, probs, arr
+    # (ii) broadcast batch
+    a = rng.uniform(-1, 1, (64, 1, 256, 256))
+    b = rng.uniform(-1, 1, (1, 32, 256, 256))
+    ta, tb = rt.asarray(a, dev), rt.asarray(b, dev)
+    tc = rt.empty((64, 32, 256, 256), np.float64, dev)
+    run = lambda: rt.matmul_into(tc, ta, tb)
+    l0 = dev.launch_count()
+    run()
+    torch.cuda.synchronize()
+    launches = dev.launch_count() - l0
+    sec = _time_events(stream, run, 3)
+    ga, gb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
+    ref = torch.matmul(ga, gb)
+    sec_ref = _time_events(stream, lambda: torch.matmul(ga, gb), 1)
+    got = torch.as_tensor(tc.to_numpy()).cuda()
+    flops = 2.0 * 2048 * 256 ** 3
+    out["c5_broadcast_batch_f64"] = {
+        "shape": "[64,1,256,256] % [1,32,256,256]", "tflops": round(flops / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
+        "rel_err_frobenius": (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item(),
+        "native_fp64_cublas_tflops": round(flops / sec_ref / 1e12, 3), "launches_per_call": int(launches)}
+    del ta, tb, tc, ga, gb, ref, got
+    torch.cuda.empty_cache()
+    # (iii) graph-captured chain
+    a = rng.uniform(-1, 1, (256, 256))
+    b = rng.uniform(-1, 1, (256, 256))
+    bias = rng.uniform(-1, 1, (256,))
+    ta, tb, tbias = rt.asarray(a, dev), rt.asarray(b, dev), rt.asarray(bias, dev)
+    c = rt.empty((256, 256), np.float64, dev)
+    o = rt.empty((256,), np.float64, dev)
+
+    def chain():
+        rt.matmul_into(c, ta, tb, 1.0, 0.0, slices=7)
+        rt.binary_inplace("add", c, tbias)
+        rt.reduce_axes_into("sum", c, [1], o)
+
+    chain()
+    eager_us = _time_events(stream, chain, 100) * 1e6
+    with rt.Graph(dev) as g:
+        chain()
+    g.launch()
+    graph_us = _time_events(stream, g.launch, 1000) * 1e6
+    want = (a @ b + bias).sum(axis=1)
+    err = float(np.linalg.norm(o.to_numpy() - want) / np.linalg.norm(want))
+    out["c5_graph_chain_f64"] = {"chain": "[256,256]%[256,256] + bias[256] -> sum_axes(1)", "replays": 1000,
+                                 "graph_us_per_iter": round(graph_us, 2), "eager_us_per_iter": round(eager_us, 2),
+                                 "rel_err": err}
+    return out
+
+
+def run_small_section(dev, stream):
+    """The small f64 row-major case: A [64,128] and b [128] uniform(-1,1),
+    B [128,96]; C = A + b, sum_axes(C, 1), argmax_axes(C, 1), A % B. Device
+    latency per operation (events, inputs resident) and the errors."""
+    import rstsr_gb300 as rt
+
+    rng = np.random.default_rng(0)
+    A = rng.uniform(-1, 1, (64, 128))
+    b = rng.uniform(-1, 1, (128,))
+    B = rng.uniform(-1, 1, (128, 96))
+    tA, tb, tB = rt.asarray(A, dev), rt.asarray(b, dev), rt.asarray(B, dev)
+    Cd = tA + tb
+    res = {}
+    res["add_us"] = round(_time_events(stream, lambda: tA + tb, 200) * 1e6, 2)
+    res["sum_axes_us"] = round(_time_events(stream, lambda: Cd.sum_axes(1), 200) * 1e6, 2)
+    res["argmax_axes_us"] = round(_time_events(stream, lambda: Cd.argmax_axes(1), 200) * 1e6, 2)
+    res["matmul_us"] = round(_time_events(stream, lambda: rt.matmul(tA, tB, slices=7), 50) * 1e6, 2)
+    C = A + b
+    res["add_bit_exact"] = bool(np.array_equal(Cd.to_numpy(), C))
+    s = Cd.sum_axes(1).to_numpy()
+    res["sum_rel_err"] = float(np.max(np.abs(s - C.sum(axis=1))) / np.max(np.abs(C.sum(axis=1))))
+    res["argmax_exact"] = bool(np.array_equal(Cd.argmax_axes(1).to_numpy(), np.argmax(C, axis=1)))
+    m = rt.matmul(tA, tB).to_numpy()
+    res["matmul_rel_err"] = float(np.linalg.norm(m - A @ B) / np.linalg.norm(A @ B))
+    return res
 
 
 def run_e2e(wl, dev, stream, args, world):
@@ -553,7 +770,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-gemm", action="store_true")
     ap.add_argument("--cpu-batch", type=int, default=4)
+    # restrict the workload (profiling a small case): comma-separated subsets
+    ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
+    ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
     args = ap.parse_args()
     if args.impl == "reference":
         res = run_reference(args)

@@ -11,6 +11,7 @@ from .tensor import (  # noqa: F401
     COL_MAJOR,
     ROW_MAJOR,
     DeviceCuda,
+    Graph,
     Tensor,
     argreduce_all,
     argreduce_axes,
@@ -28,6 +29,7 @@ from .tensor import (  # noqa: F401
     matmul_into,
     reduce_all,
     reduce_axes,
+    reduce_axes_into,
     to_contig,
     unary,
     zeros,

@@ -11,9 +11,12 @@
 // precision mode use a CUDA-core tiled kernel.
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <tuple>
 #include <vector>
 
 #include "ew_kernel.cuh"
+#include "split_gemm.hpp"
 #include "tc_gemm.cuh"
 
 namespace rstsr {
@@ -245,6 +248,89 @@ static int gemm_one(rstsr_ctx* ctx, rstsr_dtype t, const GemmProblem& q, const r
     return split_sgemm(ctx, r.M, r.N, r.K, r.alpha, A, Bt, r.beta, (float*)r.C, r.c_si, terms, r.symmetric);
 }
 
+// ------------------------------------------------------------ a batch
+
+// Several products at once. f64 / f32 with a split precision run as one
+// grouped split GEMM (one statistics, one split and one tensor-core launch
+// for the whole batch, operands shared between problems split once) when
+// every output is row- or column-major; anything else runs problem by problem.
+static int gemm_batch(rstsr_ctx* ctx, rstsr_dtype t, const std::vector<GemmProblem>& batch,
+                      const rstsr_gemm_opts* opts) {
+    if (batch.size() == 1) return gemm_one(ctx, t, batch[0], opts);
+    const int prec = opts ? opts->precision : RSTSR_PREC_AUTO;
+    const bool ozaki = t == RSTSR_F64 && (prec == RSTSR_PREC_AUTO || prec == RSTSR_PREC_OZAKI);
+    const bool bf16 = t == RSTSR_F32 && (prec == RSTSR_PREC_AUTO || prec == RSTSR_PREC_BF16X3);
+    bool grouped = ozaki || bf16;
+    std::vector<GemmProblem> rm;  // problems in row-major-output form
+    for (const GemmProblem& q : batch) {
+        if (!grouped) break;
+        if (q.M == 0 || q.N == 0) continue;
+        if (q.K == 0) {
+            grouped = false;
+            break;
+        }
+        GemmProblem r = q;
+        if (r.c_sj != 1 && r.c_si == 1) {  // column-major C: C^T = B^T A^T
+            r.M = q.N;
+            r.N = q.M;
+            r.A = q.B;
+            r.a_si = q.b_sj;
+            r.a_sk = q.b_sk;
+            r.B = q.A;
+            r.b_sk = q.a_sk;
+            r.b_sj = q.a_si;
+            r.c_si = q.c_sj;
+            r.c_sj = 1;
+        }
+        if (r.c_sj != 1 || r.c_si < r.N) {
+            grouped = false;
+            break;
+        }
+        rm.push_back(r);
+    }
+    if (!grouped) {
+        for (const GemmProblem& q : batch) {
+            int s = gemm_one(ctx, t, q, opts);
+            if (s) return s;
+        }
+        return RSTSR_OK;
+    }
+    if (rm.empty()) return RSTSR_OK;
+    // distinct operand matrices: a broadcast batch reuses them
+    std::vector<SplitItem> ai, bi;
+    std::map<std::tuple<const void*, int64_t, int64_t, int64_t, int64_t>, int> amap, bmap;
+    int rows_a = 0, rows_b = 0;
+    auto item = [](std::vector<SplitItem>& v, decltype(amap)& m, int& rows, const void* p, int64_t sr, int64_t sk,
+                   int64_t R, int64_t K) {
+        auto key = std::make_tuple(p, sr, sk, R, K);
+        auto it = m.find(key);
+        if (it != m.end()) return it->second;
+        const int idx = (int)v.size();
+        v.push_back(SplitItem{p, sr, sk, (int32_t)R, (int32_t)K, rows});
+        rows += (int)R;
+        m.emplace(key, idx);
+        return idx;
+    };
+    std::vector<SplitProblem> probs;
+    for (const GemmProblem& r : rm) {
+        if (r.M > INT32_MAX / 8 || r.N > INT32_MAX / 8 || r.K > INT32_MAX / 2)
+            return fail(RSTSR_ERR_UNIMPLEMENTED, "matrix too large for the split GEMM");
+        SplitProblem sp;
+        sp.ia = item(ai, amap, rows_a, r.A, r.a_si, r.a_sk, r.M, r.K);
+        sp.ib = item(bi, bmap, rows_b, r.B, r.b_sj, r.b_sk, r.N, r.K);  // B^T view [N, K]
+        sp.M = r.M;
+        sp.N = r.N;
+        sp.K = r.K;
+        sp.C = r.C;
+        sp.ldc = r.c_si;
+        sp.alpha = r.alpha;
+        sp.beta = r.beta;
+        probs.push_back(sp);
+    }
+    const int slices = ozaki ? (opts ? opts->ozaki_slices : 0) : (opts && opts->reserved[0] > 0 ? opts->reserved[0] : 3);
+    return split_gemm_run(ctx, ozaki ? SplitMode::Ozaki : SplitMode::Bf16x3, ai, bi, probs, slices, false);
+}
+
 // -------------------------------------------------------------- matmul
 
 static void split_at(const Layout& l, int at, Layout* rest, Layout* mat) {
@@ -357,7 +443,8 @@ static int matmul_row_major(rstsr_ctx* ctx, rstsr_dtype t, void* c, const Layout
     const char* pa = (const char*)a;
     const char* pb = (const char*)b;
     char* pc = (char*)c;
-    std::vector<int64_t> idx(std::max(cr.ndim, 1), 0);
+    std::vector<GemmProblem> batch;
+    batch.reserve((size_t)nbatch);
     for (int64_t bi = 0; bi < nbatch; ++bi) {
         int64_t oa = am.offset, ob = bm.offset, oc = cm.offset;
         if (cr.ndim > 0) {
@@ -389,10 +476,9 @@ static int matmul_row_major(rstsr_ctx* ctx, rstsr_dtype t, void* c, const Layout
         q.symmetric = syrk;
         if (M == 1 && q.c_si == 0) q.c_si = N;  // single-row views
         if (N == 1 && q.c_sj == 0) q.c_sj = 1;
-        int s = gemm_one(ctx, t, q, opts);
-        if (s) return s;
+        batch.push_back(q);
     }
-    return RSTSR_OK;
+    return gemm_batch(ctx, t, batch, opts);
 }
 
 }  // namespace rstsr
@@ -469,8 +555,14 @@ int rstsr_cuda_gemm_grouped(rstsr_ctx* ctx, rstsr_dtype t, const rstsr_gemm_prob
     clear_error();
     RSTSR_TRY(enter(ctx));
     if (nproblems < 0 || (nproblems > 0 && !problems)) return fail(RSTSR_ERR_INVALID_VALUE, "bad problem list");
+    if (!dtype_valid(t) || t == RSTSR_BOOL || t == RSTSR_F16 || t == RSTSR_BF16)
+        return fail(RSTSR_ERR_UNIMPLEMENTED, std::string("grouped GEMM is not implemented for ") + dtype_name(t));
+    std::vector<GemmProblem> batch;
     for (int i = 0; i < nproblems; ++i) {
         const rstsr_gemm_problem& g = problems[i];
+        if (g.m < 0 || g.n < 0 || g.k < 0) return fail(RSTSR_ERR_INVALID_VALUE, "negative GEMM extent");
+        if ((g.m > 0 && g.n > 0) && (!g.c || (g.k > 0 && (!g.a || !g.b))))
+            return fail(RSTSR_ERR_INVALID_VALUE, "null data pointer in problem " + std::to_string(i));
         GemmProblem q;
         q.M = g.m;
         q.N = g.n;
@@ -487,9 +579,9 @@ int rstsr_cuda_gemm_grouped(rstsr_ctx* ctx, rstsr_dtype t, const rstsr_gemm_prob
         q.alpha = g.alpha;
         q.beta = g.beta;
         q.symmetric = false;
-        RSTSR_TRY(gemm_one(ctx, t, q, opts));
+        batch.push_back(q);
     }
-    return RSTSR_OK;
+    return gemm_batch(ctx, t, batch, opts);
 }
 
 int32_t rstsr_cuda_last_ozaki_slices(void) { return last_ozaki_slices(); }

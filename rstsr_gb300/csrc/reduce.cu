@@ -209,8 +209,19 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         p.chunk = 1;
     } else if (rin <= kin) {
         // row regime
-        const int G = p.nred <= 4096 ? 32 : 256;
-        p.glog = G == 32 ? 5 : 8;
+        // group size: about four vector loads per lane for short runs, one
+        // CTA per output for long ones
+        int G = 256, glog = 8;
+        if (p.nred <= 4096) {
+            const int64_t want = (p.nred + (int64_t)VEC * 4 - 1) / ((int64_t)VEC * 4);
+            G = 1;
+            glog = 0;
+            while (G < want && G < 32) {
+                G <<= 1;
+                ++glog;
+            }
+        }
+        p.glog = glog;
         const int64_t gx = (p.nout + (kRedThreads / G) - 1) / (kRedThreads / G);
         int64_t nsplit = 1;
         if (gx < target && p.nred > (int64_t)G * VEC * 8)
@@ -229,11 +240,15 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         for (int i = 0; vec && i < p.k.nd; ++i) vec = (std::llabs(p.k.in_stride[i]) * (int64_t)es) % vb == 0;
         p.vec = vec ? 1 : 0;
     } else {
-        // column regime
+        // column regime: a warp reads 32 neighbouring outputs' elements per
+        // step (one 128/256-byte segment), so enough CTAs must be resident
+        // to keep ~40 KB per SM in flight: aim for 8 CTAs per SM
         p.glog = 0;
         const int64_t gx = (p.nout + kRedThreads - 1) / kRedThreads;
+        const int64_t col_target = 8 * (int64_t)ctx->num_sms;
         int64_t nsplit = 1;
-        if (gx < target && p.nred > 16) nsplit = std::min<int64_t>((target + gx - 1) / gx, (p.nred + 15) / 16);
+        if (gx < col_target && p.nred > 16)
+            nsplit = std::min<int64_t>((col_target + gx - 1) / gx, (p.nred + 15) / 16);
         nsplit = std::max<int64_t>(1, std::min<int64_t>(nsplit, 65535));
         int64_t chunk = (p.nred + nsplit - 1) / nsplit;
         nsplit = (p.nred + chunk - 1) / chunk;

@@ -294,23 +294,73 @@ struct RedArg {
         return (uint64_t)s.idx;
     }
 };
+// f64 arg reductions compare order-preserving int64 keys instead of doubles:
+// GB300's FP64 pipe runs at a small fraction of its integer rate, and a
+// comparison per element made the f64 argmax FP64-bound. key(x) maps -0.0 to
+// +0.0 (they compare equal) and flips the magnitude bits of negatives, so
+// x < y  <=>  key(x) < key(y) and x == y <=> key(x) == key(y) for non-NaN x, y;
+// NaN is recognised from its bits. Same results as RedArg<double>.
+template <bool IS_MAX>
+struct RedArgF64 {
+    using Acc = AccArg<int64_t>;
+    using Out = uint64_t;
+    __device__ static Acc init() { return {0, INT64_MAX, 0}; }
+    __device__ static bool better(int64_t x, int64_t ix, int64_t v, int64_t iv) {
+        if (iv == INT64_MAX) return true;
+        if (IS_MAX ? (x > v) : (x < v)) return true;
+        return x == v && ix < iv;
+    }
+    __device__ static void fold(Acc& s, double xd, int64_t lidx) {
+        int64_t b = __double_as_longlong(xd);
+        if ((b & INT64_MAX) > 0x7FF0000000000000LL) {  // NaN
+            if (lidx == 0) s.nan0 = 1;
+            return;
+        }
+        if (b == INT64_MIN) b = 0;  // -0.0 -> +0.0
+        const int64_t key = b >= 0 ? b : (b ^ INT64_MAX);
+        if (better(key, lidx, s.v, s.idx)) {
+            s.v = key;
+            s.idx = lidx;
+        }
+    }
+    __device__ static void merge(Acc& s, const Acc& o) {
+        s.nan0 |= o.nan0;
+        if (o.idx != INT64_MAX && better(o.v, o.idx, s.v, s.idx)) {
+            s.v = o.v;
+            s.idx = o.idx;
+        }
+    }
+    __device__ static Out fin(const Acc& s, int, int64_t) {
+        if (s.nan0 || s.idx == INT64_MAX) return 0;
+        return (uint64_t)s.idx;
+    }
+};
+
 template <typename T>
 struct Red<T, kRedArgMax> : RedArg<T, true> {};
 template <typename T>
 struct Red<T, kRedArgMin> : RedArg<T, false> {};
+template <>
+struct Red<double, kRedArgMax> : RedArgF64<true> {};
+template <>
+struct Red<double, kRedArgMin> : RedArgF64<false> {};
 
 // ---------------------------------------------------------------- shuffles
 
+// Shuffle within segments of `width` lanes (a power of two <= 32).
 template <typename A>
-__device__ __forceinline__ A shfl_down_acc(const A& a, int delta) {
+__device__ __forceinline__ A shfl_down_acc(const A& a, int delta, int width) {
     static_assert(sizeof(A) % 4 == 0, "accumulator must be a multiple of 4 bytes");
     A r;
     const int* src = reinterpret_cast<const int*>(&a);
     int* dst = reinterpret_cast<int*>(&r);
 #pragma unroll
-    for (int i = 0; i < (int)(sizeof(A) / 4); ++i) dst[i] = __shfl_down_sync(0xffffffffu, src[i], delta);
+    for (int i = 0; i < (int)(sizeof(A) / 4); ++i) dst[i] = __shfl_down_sync(0xffffffffu, src[i], delta, width);
     return r;
 }
+
+// loads in flight per thread in the reduction loops
+constexpr int kRedUnroll = 4;
 
 // ---------------------------------------------------------------- kernels
 
@@ -361,27 +411,49 @@ __global__ void __launch_bounds__(kRedThreads) reduce_kernel(const RedParams p) 
         }
         const int64_t rb = (int64_t)blockIdx.y * p.chunk;
         const int64_t re = min(p.nred, rb + p.chunk);
+        // kRedUnroll independent loads are issued before they are folded, so
+        // each thread keeps several requests in flight
         if (VEC > 1 && p.vec) {
-            for (int64_t r = rb + (int64_t)lane * VEC; r < re; r += (int64_t)G * VEC) {
-                int64_t li;
-                const int64_t off = red_offset(p.r, (uint32_t)r, &li);
-                const RVec<T, VEC> v = *reinterpret_cast<const RVec<T, VEC>*>(in + base + off);
+            const int64_t step = (int64_t)G * VEC;
+            for (int64_t r0 = rb + (int64_t)lane * VEC; r0 < re; r0 += step * kRedUnroll) {
+                RVec<T, VEC> v[kRedUnroll];
+                int64_t li[kRedUnroll];
 #pragma unroll
-                for (int j = 0; j < VEC; ++j) R::fold(acc, v.v[j], li + j * p.r.lstride[0]);
+                for (int u = 0; u < kRedUnroll; ++u) {
+                    const int64_t r = r0 + u * step;
+                    if (r < re) {
+                        const int64_t off = red_offset(p.r, (uint32_t)r, &li[u]);
+                        v[u] = *reinterpret_cast<const RVec<T, VEC>*>(in + base + off);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kRedUnroll; ++u) {
+                    if (r0 + u * step < re) {
+#pragma unroll
+                        for (int j = 0; j < VEC; ++j) R::fold(acc, v[u].v[j], li[u] + j * p.r.lstride[0]);
+                    }
+                }
             }
         } else {
-            for (int64_t r = rb + lane; r < re; r += G) {
-                int64_t li;
-                const int64_t off = red_offset(p.r, (uint32_t)r, &li);
-                R::fold(acc, in[base + off], li);
+            for (int64_t r0 = rb + lane; r0 < re; r0 += (int64_t)G * kRedUnroll) {
+                T x[kRedUnroll];
+                int64_t li[kRedUnroll];
+#pragma unroll
+                for (int u = 0; u < kRedUnroll; ++u) {
+                    const int64_t r = r0 + (int64_t)u * G;
+                    if (r < re) x[u] = in[base + red_offset(p.r, (uint32_t)r, &li[u])];
+                }
+#pragma unroll
+                for (int u = 0; u < kRedUnroll; ++u)
+                    if (r0 + (int64_t)u * G < re) R::fold(acc, x[u], li[u]);
             }
         }
     }
     // combine the group (fixed tree: deterministic)
-    if (G >= 32) {
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
-            Acc other = shfl_down_acc(acc, d);
+    if (G > 1) {
+        const int width = G < 32 ? G : 32;
+        for (int d = width >> 1; d > 0; d >>= 1) {
+            Acc other = shfl_down_acc(acc, d, width);
             R::merge(acc, other);
         }
         if (G > 32) {

@@ -695,6 +695,52 @@ def argreduce_axes(is_max: bool, t: Tensor, axes) -> Tensor:
     return Tensor(st, lout.shape_t, lout.stride_t, lout.offset, _lib.U64)
 
 
+# ------------------------------------------------------------------- graphs
+
+
+class Graph:
+    """Capture the library calls made on a device into one CUDA graph.
+
+    with Graph(dev) as g:
+        ...calls on dev...
+    g.launch()   # replays every captured kernel with one launch
+    """
+
+    def __init__(self, device: DeviceCuda):
+        self.device = device
+        self.handle = C.c_void_p()
+
+    def __enter__(self) -> "Graph":
+        call("rstsr_cuda_graph_begin", self.device.ctx)
+        return self
+
+    def __exit__(self, exc_type, exc, tb):
+        h = C.c_void_p()
+        rc = lib().rstsr_cuda_graph_end(self.device.ctx, C.byref(h))
+        self.handle = h
+        if exc_type is None:
+            check(rc)
+
+    def launch(self) -> None:
+        call("rstsr_cuda_graph_launch", self.device.ctx, self.handle)
+
+    def __del__(self):  # pragma: no cover
+        try:
+            if self.handle and self.handle.value:
+                lib().rstsr_cuda_graph_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def reduce_axes_into(op: str, t: Tensor, axes, out: Tensor) -> Tensor:
+    arr, n = _axes_arg(t, axes)
+    call(
+        "rstsr_cuda_reduce_axes_into", t.device.ctx, _lib.RED[op], t.dtype_code, C.c_void_p(t.ptr),
+        C.byref(t.layout()), arr, n, C.c_void_p(out.ptr), C.byref(out.layout()),
+    )
+    return out
+
+
 # ------------------------------------------------------------------- matmul
 
 

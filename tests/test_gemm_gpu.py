@@ -206,3 +206,71 @@ def test_zero_k_scales_c(dev):
     b = rt.zeros((0, 5), np.float64, dev)
     rt.matmul_into(c, a, b, 1.0, 0.5)
     assert (c.to_numpy() == 1.0).all()
+
+
+def test_broadcast_batched_matmul_one_launch(dev):
+    """Rule 7 broadcast batch [8,1,96,64] % [1,5,64,80] (40 products) runs as
+    one grouped split GEMM; every product within the f64 bar."""
+    rng = np.random.default_rng(8)
+    a = rng.uniform(-1, 1, (8, 1, 96, 64))
+    b = rng.uniform(-1, 1, (1, 5, 64, 80))
+    l0 = dev.launch_count()
+    got = (rt.asarray(a, dev) % rt.asarray(b, dev)).to_numpy()
+    launches = dev.launch_count() - l0
+    assert launches <= 12, f"{launches} launches for one batched matmul"
+    assert got.shape == (8, 5, 96, 80)
+    assert rel_err(got, np.matmul(a, b)) <= F64_TOL
+    af = a.astype(np.float32)
+    bf = b.astype(np.float32)
+    gotf = (rt.asarray(af, dev) % rt.asarray(bf, dev)).to_numpy()
+    assert rel_err(gotf, np.matmul(af.astype(np.float64), bf.astype(np.float64))) <= F32_TOL
+
+
+def test_grouped_uneven_f32_and_transposed_outputs(dev):
+    rng = np.random.default_rng(9)
+    from rstsr_gb300._lib import GemmProblem
+
+    probs, keep = [], []
+    for i in range(9):
+        m, n, k = (int(x) for x in rng.integers(16, 300, 3))
+        a = rng.uniform(-1, 1, (m, k)).astype(np.float32)
+        b = rng.uniform(-1, 1, (k, n)).astype(np.float32)
+        ta, tb = rt.asarray(a, dev), rt.asarray(b, dev)
+        tc = rt.full((m, n), 1.0, np.float32, dev)
+        keep.append((a, b, ta, tb, tc))
+        probs.append(GemmProblem(m, n, k, k, n, n, ta.ptr, tb.ptr, tc.ptr, 2.0, -1.0))
+    arr = (GemmProblem * len(probs))(*probs)
+    call("rstsr_cuda_gemm_grouped", dev.ctx, 1, arr, len(probs), None)
+    for a, b, _, _, tc in keep:
+        want = 2.0 * (a.astype(np.float64) @ b.astype(np.float64)) - 1.0
+        assert rel_err(tc.to_numpy(), want) <= F32_TOL
+
+
+def test_graph_captured_chain_matches_eager(dev):
+    """matmul -> broadcast bias add -> sum_axes captured once, replayed."""
+    rng = np.random.default_rng(10)
+    a = rng.uniform(-1, 1, (256, 256))
+    b = rng.uniform(-1, 1, (256, 256))
+    bias = rng.uniform(-1, 1, (256,))
+    ta, tb, tbias = rt.asarray(a, dev), rt.asarray(b, dev), rt.asarray(bias, dev)
+    c = rt.empty((256, 256), np.float64, dev)
+    out = rt.empty((256,), np.float64, dev)
+
+    def chain():
+        rt.matmul_into(c, ta, tb, 1.0, 0.0, slices=7)
+        rt.binary_inplace("add", c, tbias)
+        rt.reduce_axes_into("sum", c, [1], out)
+
+    chain()  # eager warm-up
+    eager = out.to_numpy().copy()
+    with rt.Graph(dev) as g:
+        chain()
+    rt.fill(out, 0.0)
+    n0 = dev.launch_count()
+    for _ in range(5):
+        g.launch()
+    dev.sync()
+    assert dev.launch_count() - n0 >= 5 * 3
+    np.testing.assert_array_equal(out.to_numpy(), eager)
+    want = (a @ b + bias).sum(axis=1)
+    assert rel_err(eager, want) <= F64_TOL
