@@ -307,7 +307,7 @@ static int gemm_batch(rstsr_ctx* ctx, rstsr_dtype t, const std::vector<GemmProbl
         if (it != m.end()) return it->second;
         const int idx = (int)v.size();
         v.push_back(SplitItem{p, sr, sk, (int32_t)R, (int32_t)K, rows});
-        rows += (int)R;
+        rows += (int)((R + 7) / 8 * 8);  // items start on 8-row groups of the tile layout
         m.emplace(key, idx);
         return idx;
     };

@@ -16,14 +16,16 @@
 // cores accumulate FP32 by truncation, so the merged accumulator errs by one
 // unit of its last place per step; starting it at level 4 keeps that below
 // 2^-51 of the result per step. Only levels s + t < L are formed.
-// The epilogue adds the accumulators in double and rescales by
-// 2^(e_i + f_j - 14).
+// The epilogue adds the accumulators in 64-bit fixed point and rescales by
+// 2^(e_i + f_j - 14). Statistics, slicing and epilogue use integer arithmetic
+// on the doubles' bits: GB300's FP64 rate is a small fraction of its integer
+// rate, and FP64 instructions per element bounded every stage before.
 //
 // f32 (three-term bf16 split): Henry, Tang & Heinecke, "Leveraging the
 // bfloat16 artificial intelligence datatype for higher-precision computations",
 // ARITH 2019. x = hi + mid + lo exactly (8 bits each); the six products with
 // term order <= 2 (hi*hi | hi*mid + mid*hi | hi*lo + mid*mid + lo*hi)
-// accumulate in three FP32 accumulators and are summed in double.
+// accumulate in three FP32 accumulators, summed in FP32 with a two-sum.
 //
 // Work is described as a list of problems over a list of distinct operand
 // matrices ("items"): one matrix product, a broadcast batch (rule 7 of the
@@ -55,86 +57,147 @@ __device__ __forceinline__ SplitItem seg_at(const SegArg& a, int i) { return a.n
 
 // ------------------------------------------------------------- statistics
 
-// Per-row max |x| (ordered uint64 bits of a non-negative double) and sum |x|.
+// The A items and the B items of one call are handled by the same launches:
+// blockIdx.z < a.n selects an A item, the rest select B items, whose rows
+// follow the A rows (rows_a of them) in the statistics arrays.
+struct SegPair {
+    SegArg a, b;
+    int32_t rows_a;
+};
+
+__device__ __forceinline__ SplitItem pair_item(const SegPair& sp, int z, bool& is_b) {
+    is_b = z >= sp.a.n;
+    return is_b ? seg_at(sp.b, z - sp.a.n) : seg_at(sp.a, z);
+}
+
+// GB300 executes FP64 arithmetic at a small fraction of its integer and FP32
+// rates, so the statistics, the split and the GEMM epilogue work on the bit
+// patterns of the doubles wherever they can: |x| is the value's bits with the
+// sign cleared, whose integer order is the order of the values.
+
+// e such that m < 2^e for the row maximum m given as |x| bits (0 for zero).
+__device__ __forceinline__ int exp_above(unsigned long long b) {
+    const int E = (int)(b >> 52);
+    if (E != 0) return E - 1022;
+    if (b == 0) return 0;
+    return -1010 - __clzll((long long)b);  // subnormal: highest set bit p, m < 2^(p - 1073)
+}
+
+// Per-row max |x| (as |x| bits) and sum |x|.
 template <typename T>
-__global__ void __launch_bounds__(256) row_stats_kernel(const SegArg segs, unsigned long long* __restrict__ maxbits,
+__global__ void __launch_bounds__(256) row_stats_kernel(const SegPair segs, unsigned long long* __restrict__ maxbits,
                                                         double* __restrict__ sumabs) {
-    const SplitItem it = seg_at(segs, blockIdx.z);
+    bool is_b;
+    const SplitItem it = pair_item(segs, blockIdx.z, is_b);
     const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
     if (r0 >= it.R || k0 >= it.K) return;  // uniform per block
-    __shared__ double smax[8][33];
+    const int base = (is_b ? segs.rows_a : 0) + it.row0;
+    __shared__ unsigned long long smax[8][33];
     __shared__ double ssum[8][33];
     const T* X = (const T*)it.ptr;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const bool kfast = it.s_k == 1 || (it.s_row != 1 && llabs(it.s_k) <= llabs(it.s_row));
-    double m[4] = {0, 0, 0, 0}, s[4] = {0, 0, 0, 0};
+    unsigned long long m[4] = {0, 0, 0, 0};
+    double s[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int rr = kfast ? ty + 8 * j : tx;
         const int kk = kfast ? tx : ty + 8 * j;
         const int r = r0 + rr, k = k0 + kk;
         if (r < it.R && k < it.K) {
-            const double v = fabs((double)X[(int64_t)r * it.s_row + (int64_t)k * it.s_k]);
-            m[j] = v;
-            s[j] = v;
+            const unsigned long long b =
+                (unsigned long long)__double_as_longlong((double)X[(int64_t)r * it.s_row + (int64_t)k * it.s_k]) &
+                0x7FFFFFFFFFFFFFFFull;
+            m[j] = b;
+            s[j] = __longlong_as_double((long long)b);
         }
     }
     if (kfast) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            double mm = m[j], ss = s[j];
+            unsigned long long mm = m[j];
+            double ss = s[j];
             for (int d = 16; d > 0; d >>= 1) {
-                mm = fmax(mm, __shfl_down_sync(0xffffffffu, mm, d));
+                const unsigned long long o = __shfl_down_sync(0xffffffffu, mm, d);
+                mm = o > mm ? o : mm;
                 ss += __shfl_down_sync(0xffffffffu, ss, d);
             }
             const int r = r0 + ty + 8 * j;
             if (tx == 0 && r < it.R) {
-                atomicMax(&maxbits[it.row0 + r], (unsigned long long)__double_as_longlong(mm));
-                atomicAdd(&sumabs[it.row0 + r], ss);
+                atomicMax(&maxbits[base + r], mm);
+                atomicAdd(&sumabs[base + r], ss);
             }
         }
     } else {
-        double mm = fmax(fmax(m[0], m[1]), fmax(m[2], m[3]));
+        unsigned long long mm = m[0];
+        for (int j = 1; j < 4; ++j) mm = m[j] > mm ? m[j] : mm;
         double ss = s[0] + s[1] + s[2] + s[3];
         smax[ty][tx] = mm;
         ssum[ty][tx] = ss;
         __syncthreads();
         if (ty == 0) {
             for (int i = 1; i < 8; ++i) {
-                mm = fmax(mm, smax[i][tx]);
+                mm = smax[i][tx] > mm ? smax[i][tx] : mm;
                 ss += ssum[i][tx];
             }
             const int r = r0 + tx;
             if (r < it.R) {
-                atomicMax(&maxbits[it.row0 + r], (unsigned long long)__double_as_longlong(mm));
-                atomicAdd(&sumabs[it.row0 + r], ss);
+                atomicMax(&maxbits[base + r], mm);
+                atomicAdd(&sumabs[base + r], ss);
             }
         }
     }
 }
 
-// e_r such that max_r < 2^e_r (0 for an all-zero row)
-__global__ void exps_kernel(const unsigned long long* __restrict__ maxbits, int R, int32_t* __restrict__ exps) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= R) return;
-    const double m = __longlong_as_double((long long)maxbits[r]);
-    int e = 0;
-    if (m > 0) frexp(m, &e);
-    exps[r] = e;
-}
-
 // ------------------------------------------------------------------ split
 
-// Cut every item into slices, written K-major into the stack as
-// out[s * plane + (row0 + r) * pitch + k] (bf16), zero in [K, pitch).
-// MODE 0: Ozaki integer slices of x * 2^-e_r, slice s stored as d_s 2^(-7s).
+// Ozaki slices of one double x of a row with exponent e_r: y = x 2^-e_r as the
+// fixed-point integer Y = y 2^63 (|Y| < 2^63; bits below 2^-63 of the row
+// maximum are dropped), then balanced base-128 digits from the top,
+// d_s = round(Y / 2^(56 - 7s)) with Y reduced by each digit, so that
+// |d_0| <= 128 and |d_s| <= 64 after it. Slice s is stored as d_s 2^(-7s),
+// exact in bf16. Non-finite x puts itself in slice 0 and zeros after it.
+__device__ __forceinline__ void ozaki_digits(double x, int e_r, int S, __nv_bfloat16* out, size_t plane) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((u >> 52) & 0x7FF);
+    if (E == 0x7FF) {
+        const uint32_t nan = (u & 0xFFFFFFFFFFFFFull) ? 0x7FC00000u : 0x7F800000u;
+        out[0] = __float2bfloat16_rn(__uint_as_float((uint32_t)(u >> 32) & 0x80000000u | nan));
+        for (int s = 1; s < S; ++s) out[s * plane] = __float2bfloat16_rn(0.f);
+        return;
+    }
+    const long long mant = (long long)(E ? (u & 0xFFFFFFFFFFFFFull) | (1ull << 52) : (u & 0xFFFFFFFFFFFFFull));
+    const int sh = (E ? E : 1) - 1012 - e_r;  // |x| = mant 2^((E ? E : 1) - 1075) < 2^e_r, so Y < 2^63
+    long long Y = sh >= 0 ? mant << sh : (sh > -63 ? mant >> -sh : 0);
+    if (u >> 63) Y = -Y;
+    for (int s = 0; s < S; ++s) {
+        const int k = 56 - 7 * s;
+        const long long d = (Y >> k) + ((Y >> (k - 1)) & 1);  // round half up, no overflow
+        Y -= d << k;
+        out[s * plane] = __float2bfloat16_rn(__int2float_rn((int)d) * __int_as_float((127 - 7 * s) << 23));
+    }
+}
+
+// Cut every item into slices, written into the stack of its side in the
+// tensor-core tile layout (tc_tiled_offset with KT = 2^lkt and G row groups:
+// slice s of element (row, k) lies s * G * 8 * KT after slice 0), zero in
+// [K, pitch).
+// MODE 0: Ozaki integer slices (ozaki_digits); the k-tile-0 blocks also store
+//         the row exponents e_r (max_r < 2^e_r) from the row maxima.
 // MODE 1: f32 three-term split hi / mid / lo.
 template <typename T, int MODE>
-__global__ void __launch_bounds__(256) split_kernel(const SegArg segs, int pitch, int S, size_t plane,
-                                                    const int32_t* __restrict__ exps, __nv_bfloat16* __restrict__ out) {
-    const SplitItem it = seg_at(segs, blockIdx.z);
+__global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitch, int S, int lkt, int groups_a,
+                                                    int groups_b, const unsigned long long* __restrict__ maxbits,
+                                                    int32_t* __restrict__ exps, __nv_bfloat16* __restrict__ out_a,
+                                                    __nv_bfloat16* __restrict__ out_b) {
+    bool is_b;
+    const SplitItem it = pair_item(segs, blockIdx.z, is_b);
     const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
     if (r0 >= it.R || k0 >= pitch) return;  // uniform per block
+    const int G = is_b ? groups_b : groups_a;
+    const size_t plane = (size_t)G << (3 + lkt);
+    __nv_bfloat16* out = is_b ? out_b : out_a;
+    const int base = (is_b ? segs.rows_a : 0) + it.row0;  // statistics row of r = 0
     __shared__ T tile[32][33];
     const T* X = (const T*)it.ptr;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -154,19 +217,17 @@ __global__ void __launch_bounds__(256) split_kernel(const SegArg segs, int pitch
         const int rr = ty + 8 * j;
         const int r = r0 + rr, k = k0 + tx;
         if (r >= it.R || k >= pitch) continue;
-        const size_t o = (size_t)(it.row0 + r) * pitch + k;
+        const int row = it.row0 + r;
+        const size_t o = ((((size_t)(k >> lkt) * S) * G + (size_t)(row >> 3)) << (3 + lkt)) +
+                         (size_t)((((k & ((1 << lkt) - 1)) >> 3) << 6) + ((row & 7) << 3) + (k & 7));
         if (k >= it.K) {
             for (int s = 0; s < S; ++s) out[s * plane + o] = __float2bfloat16_rn(0.f);
             continue;
         }
         if constexpr (MODE == 0) {
-            double y = ldexp((double)tile[rr][tx], -exps[it.row0 + r]);
-            for (int s = 0; s < S; ++s) {
-                const double t = y * 128.0;  // exact
-                const double d = rint(t);    // |d| <= 128
-                out[s * plane + o] = __double2bfloat16(ldexp(d, -7 * s));  // exact: 8-bit integer
-                y = t - d;                   // exact
-            }
+            const int e_r = exp_above(maxbits[base + r]);
+            if (k == 0) exps[base + r] = e_r;
+            ozaki_digits((double)tile[rr][tx], e_r, S, out + o, plane);
         } else {
             const float x = (float)tile[rr][tx];
             const __nv_bfloat16 hi = __float2bfloat16_rn(x);
@@ -183,7 +244,17 @@ __global__ void __launch_bounds__(256) split_kernel(const SegArg segs, int pitch
 
 // ------------------------------------------------------------------ driver
 
-static int kt_for_slices(int s) { return s <= 7 ? (s <= 3 ? 64 : 32) : 16; }
+// K tile width: the widest of 64 / 32 / 16 whose pipeline stage (every slice
+// of a 128-row A tile and a BN-row B tile) leaves room for four stages, so
+// that TMA latency stays hidden behind the products of the other stages.
+static int kt_for_stages(int slices, int bn) {
+    const size_t budget = kTcSmemMax - 1024 - kTcSmemTail;
+    for (int kt : {64, 32}) {
+        const size_t stage = (size_t)slices * (kTcBM + bn) * kt * 2;
+        if (budget / stage >= 4) return kt;
+    }
+    return 16;
+}
 
 // Slices needed for <= 1e-12 relative error given the spread (log2 of row
 // max over row mean |x|) of both operands. Dropping the levels >= L leaves an
@@ -225,10 +296,11 @@ static int make_segs(rstsr_ctx* ctx, const std::vector<SplitItem>& items, SegArg
     return s;
 }
 
-static void grid_for(const std::vector<SplitItem>& items, int pitch, dim3* g) {
+static dim3 grid_for(const std::vector<SplitItem>& a, const std::vector<SplitItem>& b, int width) {
     int maxr = 1;
-    for (const auto& it : items) maxr = std::max(maxr, it.R);
-    *g = dim3((unsigned)((pitch + 31) / 32), (unsigned)((maxr + 31) / 32), (unsigned)items.size());
+    for (const auto& it : a) maxr = std::max(maxr, it.R);
+    for (const auto& it : b) maxr = std::max(maxr, it.R);
+    return dim3((unsigned)((width + 31) / 32), (unsigned)((maxr + 31) / 32), (unsigned)(a.size() + b.size()));
 }
 
 int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>& a_items,
@@ -240,7 +312,6 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     for (const auto& it : a_items) rows_a = std::max(rows_a, it.row0 + it.R), maxk = std::max(maxk, it.K);
     for (const auto& it : b_items) rows_b = std::max(rows_b, it.row0 + it.R), maxk = std::max(maxk, it.K);
     if (items_too_large(rows_a, rows_b, maxk)) return fail(RSTSR_ERR_UNIMPLEMENTED, "operands too large for the split GEMM");
-    const int pitch = (maxk + 7) / 8 * 8;
     if (symmetric && (probs.size() != 1 || !b_items.empty()))
         return fail(RSTSR_ERR_RUNTIME, "symmetric split GEMM takes one problem and the A operand only");
     std::vector<void*> owned;
@@ -248,36 +319,29 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
         for (void* p : owned) scratch_free(ctx, p);
     };
     int s = RSTSR_OK;
-    SegArg sa_arg, sb_arg;
+    SegPair segs;
+    memset(&segs, 0, sizeof(segs));
+    segs.rows_a = rows_a;
     void* dseg = nullptr;
-    if ((s = make_segs(ctx, a_items, &sa_arg, &dseg))) return cleanup(), s;
+    if ((s = make_segs(ctx, a_items, &segs.a, &dseg))) return cleanup(), s;
     if (dseg) owned.push_back(dseg);
-    if ((s = make_segs(ctx, b_items, &sb_arg, &dseg))) return cleanup(), s;
+    if ((s = make_segs(ctx, b_items, &segs.b, &dseg))) return cleanup(), s;
     if (dseg) owned.push_back(dseg);
-    // per-row statistics and exponents (Ozaki only)
+    // per-row statistics (Ozaki only); B rows follow A rows
     const size_t nst = (size_t)rows_a + rows_b;
     int32_t* exps = nullptr;
+    unsigned long long* maxbits = nullptr;
     int L;
     if (f64) {
         void* stats = nullptr;
         if ((s = scratch_alloc(ctx, nst * (8 + 8 + 4), &stats))) return cleanup(), s;
         owned.push_back(stats);
-        auto* maxbits = (unsigned long long*)stats;
+        maxbits = (unsigned long long*)stats;
         auto* sumabs = (double*)(maxbits + nst);
         exps = (int32_t*)(sumabs + nst);
-        cudaMemsetAsync(stats, 0, nst * 16, ctx->stream);
-        dim3 g;
-        grid_for(a_items, maxk, &g);
-        row_stats_kernel<double><<<g, 256, 0, ctx->stream>>>(sa_arg, maxbits, sumabs);
+        RSTSR_CUDA_TRY(cudaMemsetAsync(stats, 0, nst * 16, ctx->stream));
+        row_stats_kernel<double><<<grid_for(a_items, b_items, maxk), 256, 0, ctx->stream>>>(segs, maxbits, sumabs);
         if ((s = after_launch(ctx, "row_stats_kernel"))) return cleanup(), s;
-        if (!b_items.empty()) {
-            grid_for(b_items, maxk, &g);
-            // B rows follow A rows in the statistics arrays
-            row_stats_kernel<double><<<g, 256, 0, ctx->stream>>>(sb_arg, maxbits + rows_a, sumabs + rows_a);
-            if ((s = after_launch(ctx, "row_stats_kernel"))) return cleanup(), s;
-        }
-        exps_kernel<<<(unsigned)((nst + 255) / 256), 256, 0, ctx->stream>>>(maxbits, (int)nst, exps);
-        if ((s = after_launch(ctx, "exps_kernel"))) return cleanup(), s;
         L = slices;
         bool capturing = false;
         cudaStreamCaptureStatus cs;
@@ -312,59 +376,61 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     }
     g_last_slices = f64 ? L : 0;
     const int S = L;
-    // slices
+    constexpr int BN = kTcBN;
+    const int kt = kt_for_stages(S, BN);
+    const int lkt = kt == 64 ? 6 : kt == 32 ? 5 : 4;
+    const int pitch = (maxk + kt - 1) / kt * kt;
+    // slice stacks in the tile layout; row groups past the last row cover the
+    // rows a 128-row A tile or 64-row B tile may read beyond it
+    const int groups_a = (rows_a + 7) / 8 + kTcBM / 8, groups_b = (rows_b + 7) / 8 + kTcBM / 8;
+    const size_t stack_a = (size_t)S * pitch * groups_a * 8, stack_b = b_items.empty() ? 0 : (size_t)S * pitch * groups_b * 8;
     void* sl = nullptr;
-    const size_t plane_a = (size_t)rows_a * pitch, plane_b = (size_t)rows_b * pitch;
-    if ((s = scratch_alloc(ctx, ((size_t)S * (plane_a + plane_b)) * 2, &sl))) return cleanup(), s;
+    if ((s = scratch_alloc(ctx, (stack_a + stack_b) * 2, &sl))) return cleanup(), s;
     owned.push_back(sl);
     auto* as = (__nv_bfloat16*)sl;
-    auto* bs = b_items.empty() ? as : as + (size_t)S * plane_a;
+    auto* bs = b_items.empty() ? as : as + stack_a;
     {
-        dim3 g;
-        grid_for(a_items, pitch, &g);
+        const dim3 g = grid_for(a_items, b_items, pitch);
         if (f64)
-            split_kernel<double, 0><<<g, 256, 0, ctx->stream>>>(sa_arg, pitch, S, plane_a, exps, as);
+            split_kernel<double, 0>
+                <<<g, 256, 0, ctx->stream>>>(segs, pitch, S, lkt, groups_a, groups_b, maxbits, exps, as, bs);
         else
-            split_kernel<float, 1><<<g, 256, 0, ctx->stream>>>(sa_arg, pitch, S, plane_a, nullptr, as);
+            split_kernel<float, 1>
+                <<<g, 256, 0, ctx->stream>>>(segs, pitch, S, lkt, groups_a, groups_b, nullptr, nullptr, as, bs);
         if ((s = after_launch(ctx, "split_kernel"))) return cleanup(), s;
-        if (!b_items.empty()) {
-            grid_for(b_items, pitch, &g);
-            if (f64)
-                split_kernel<double, 0><<<g, 256, 0, ctx->stream>>>(sb_arg, pitch, S, plane_b, exps + rows_a, bs);
-            else
-                split_kernel<float, 1><<<g, 256, 0, ctx->stream>>>(sb_arg, pitch, S, plane_b, nullptr, bs);
-            if ((s = after_launch(ctx, "split_kernel"))) return cleanup(), s;
-        }
     }
     // products and accumulators
     TcGemmParams p;
     memset(&p, 0, sizeof(p));
     p.sa = S;
     p.sb = S;
-    p.a_rows = rows_a;
-    p.b_rows = b_items.empty() ? rows_a : rows_b;
-    int np = 0;
-    for (int l = 0; l < L; ++l)
-        for (int a = 0; a <= l; ++a) {
-            const int b = l - a;
-            if (a >= S || b >= S) continue;
-            p.prod_a[np] = (uint8_t)a;
-            p.prod_b[np] = (uint8_t)b;
-            p.prod_acc[np] = (uint8_t)(f64 ? std::min(l, 4) : l);
-            ++np;
+    p.a_stack = as;
+    p.b_stack = bs;
+    p.a_groups = groups_a;
+    p.b_groups = b_items.empty() ? groups_a : groups_b;
+    // products A_a B_b with a + b < L, level a + b in TMEM slot a + b: for each
+    // A slice, its B slices 0 .. L-1-a in runs of up to four per MMA
+    int nm = 0;
+    for (int a = 0; a < S && a < L; ++a) {
+        const int nb = std::min(S, L - a);
+        for (int b0 = 0; b0 < nb; b0 += kTcMaxStack) {
+            if (nm >= kTcMaxMma) return cleanup(), fail(RSTSR_ERR_UNIMPLEMENTED, "too many slices");
+            p.mma_a[nm] = (uint8_t)a;
+            p.mma_b0[nm] = (uint8_t)b0;
+            p.mma_n[nm] = (uint8_t)std::min(kTcMaxStack, nb - b0);
+            ++nm;
         }
-    p.nprod = np;
-    p.nacc = f64 ? std::min(L, 5) : S;
+    }
+    p.nmma = nm;
+    p.nslots = L;
     p.out_f64 = f64 ? 1 : 0;
     p.exp_bias = -14;
     p.row_exp = exps;
     p.col_exp = exps ? (b_items.empty() ? exps : exps + rows_a) : nullptr;
     p.err = ctx->dev_err;
-    const int kt = f64 ? kt_for_slices(S) : 64;
-    // FP32 accumulation truncates: Ozaki chunks of <= 1024 keep levels 0 and 1
+    // FP32 accumulation truncates: Ozaki chunks of <= 1024 keep levels 0 to 3
     // exact; the f32 split sums chunks of 512 in C
     const int chunk = f64 ? std::max(1, 1024 / kt) : 512 / kt;
-    const int BN = p.nacc > 4 ? 96 : 128;
     int k_tiles_max = 0;
     for (const auto& q : probs) k_tiles_max = std::max<int>(k_tiles_max, (int)((q.K + kt - 1) / kt));
     if (probs.size() == 1) {
@@ -381,7 +447,7 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
         if (ia.row0 != 0 || ib.row0 != 0) {
             // one problem inside a larger stack: use the grouped form
         } else {
-            s = launch_tc_gemm(ctx, kt, as, bs, (uint64_t)pitch, p, k_tiles_max, chunk);
+            s = launch_tc_gemm(ctx, kt, p, k_tiles_max, chunk);
             return cleanup(), s;
         }
     }
@@ -417,8 +483,7 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     owned.push_back(dtiles);
     p.problems = (const TcProblem*)dprob;
     p.tiles = (const int4*)dtiles;
-    p.kt_count = chunk;
-    s = launch_tc_gemm(ctx, kt, as, bs, (uint64_t)pitch, p, k_tiles_max, chunk, (int64_t)tiles.size());
+    s = launch_tc_gemm(ctx, kt, p, k_tiles_max, chunk, (int64_t)tiles.size());
     return cleanup(), s;
 }
 

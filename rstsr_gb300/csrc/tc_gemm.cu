@@ -1,90 +1,53 @@
-// Host launcher of the multi-product tcgen05 GEMM (tc_gemm.cuh) and its TMA
-// tensor maps.
+// Host launcher of the multi-product tcgen05 GEMM (tc_gemm.cuh).
 #include <algorithm>
+#include <atomic>
 #include <cstring>
-
-#include <cudaTypedefs.h>
 
 #include "tc_gemm.cuh"
 
 namespace rstsr {
 
-// cuTensorMapEncodeTiled is resolved through the runtime's driver entry point
-// so that the library does not link libcuda directly (it still loads, for the
-// host-only entry points, on machines without a driver).
-static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+template <int KT, bool F64>
+static int launch_kt(rstsr_ctx* ctx, const TcGemmParams& p, unsigned grid) {
+    const size_t smem = (size_t)p.stages * p.stage_bytes + 1024 /*align*/ + kTcSmemTail;
+    grid = std::min<unsigned>(grid, (unsigned)std::max(ctx->num_sms, 1));  // persistent: one CTA per SM
+    static std::atomic<uint64_t> attr_set{0};  // bit d: opted in on device d
+    const uint64_t bit = 1ull << (ctx->device & 63);
+    if (!(attr_set.load() & bit)) {
+        RSTSR_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel<KT, kTcBN, F64>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemMax));
+        attr_set.fetch_or(bit);
     }
-    return fn;
-}
-
-int make_bf16_tma(CUtensorMap* map, const void* base, uint64_t rows, uint64_t cols, uint64_t pitch_elems, int kt,
-                  int box_rows) {
-    memset(map, 0, sizeof(*map));
-    if ((reinterpret_cast<uintptr_t>(base) & 15) || (pitch_elems * 2) % 16)
-        return fail(RSTSR_ERR_RUNTIME, "TMA operand not 16-byte aligned");
-    auto encode = encode_fn();
-    if (!encode) return fail(RSTSR_ERR_DEVICE, "cuTensorMapEncodeTiled is not available from the driver");
-    cuuint64_t dims[2] = {cols, rows};
-    cuuint64_t strides[1] = {pitch_elems * 2};
-    cuuint32_t box[2] = {(cuuint32_t)kt, (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUtensorMapSwizzle sw = kt == 64   ? CU_TENSOR_MAP_SWIZZLE_128B
-                            : kt == 32 ? CU_TENSOR_MAP_SWIZZLE_64B
-                                       : CU_TENSOR_MAP_SWIZZLE_32B;
-    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-                        CU_TENSOR_MAP_INTERLEAVE_NONE, sw, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS)
-        return fail(RSTSR_ERR_DEVICE, "cuTensorMapEncodeTiled failed with CUresult " + std::to_string((int)r));
-    return RSTSR_OK;
-}
-
-template <int KT, int BN>
-static int launch_kt(rstsr_ctx* ctx, const CUtensorMap& ma, const CUtensorMap& mb, const TcGemmParams& p,
-                     unsigned grid) {
-    const size_t smem = (size_t)p.stages * p.stage_bytes + 1024 /*align*/ + 256 /*barriers*/;
-    static bool attr_set = false;
-    if (!attr_set) {
-        RSTSR_CUDA_TRY(
-            cudaFuncSetAttribute(tc_gemm_kernel<KT, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
-        attr_set = true;
-    }
-    tc_gemm_kernel<KT, BN><<<grid, kTcThreads, smem, ctx->stream>>>(ma, mb, p);
+    tc_gemm_kernel<KT, kTcBN, F64><<<grid, kTcThreads, smem, ctx->stream>>>(p);
     return after_launch(ctx, "tc_gemm_kernel");
 }
 
-template <int BN>
-static int launch_bn(rstsr_ctx* ctx, int kt, const CUtensorMap& ma, const CUtensorMap& mb, const TcGemmParams& p,
-                     unsigned grid) {
+template <bool F64>
+static int launch_out(rstsr_ctx* ctx, int kt, const TcGemmParams& p, unsigned grid) {
     switch (kt) {
-        case 64: return launch_kt<64, BN>(ctx, ma, mb, p, grid);
-        case 32: return launch_kt<32, BN>(ctx, ma, mb, p, grid);
-        default: return launch_kt<16, BN>(ctx, ma, mb, p, grid);
+        case 64: return launch_kt<64, F64>(ctx, p, grid);
+        case 32: return launch_kt<32, F64>(ctx, p, grid);
+        default: return launch_kt<16, F64>(ctx, p, grid);
     }
 }
 
-int launch_tc_gemm(rstsr_ctx* ctx, int kt, const void* a_slices, const void* b_slices, uint64_t kp, TcGemmParams p,
-                   int k_tiles_total, int k_chunk_tiles, int64_t ntiles_grouped) {
-    const int BN = p.nacc > 4 ? 96 : 128;
-    if (p.nacc > kTcMaxAcc || p.nacc * BN > (int)kTcTmemCols)
-        return fail(RSTSR_ERR_UNIMPLEMENTED, "too many TMEM accumulators");
-    CUtensorMap ma, mb;
-    int s = make_bf16_tma(&ma, a_slices, (uint64_t)p.sa * p.a_rows, kp, kp, kt, kTcBM);
-    if (s) return s;
-    s = make_bf16_tma(&mb, b_slices, (uint64_t)p.sb * p.b_rows, kp, kp, kt, BN);
-    if (s) return s;
+int launch_tc_gemm(rstsr_ctx* ctx, int kt, TcGemmParams p, int k_tiles_total, int k_chunk_tiles,
+                   int64_t ntiles_grouped) {
+    constexpr int BN = kTcBN;
+    if (kt != 16 && kt != 32 && kt != 64) return fail(RSTSR_ERR_RUNTIME, "K tile must be 16, 32 or 64");
+    if (p.nslots < 1 || p.nslots > kTcMaxSlots || p.nslots * BN > (int)kTcTmemCols)
+        return fail(RSTSR_ERR_UNIMPLEMENTED, "too many TMEM level slots");
+    if (p.nmma < 1 || p.nmma > kTcMaxMma) return fail(RSTSR_ERR_UNIMPLEMENTED, "too many MMAs per K step");
+    for (int q = 0; q < p.nmma; ++q)
+        if (p.mma_n[q] < 1 || p.mma_n[q] > kTcMaxStack || p.mma_a[q] >= p.sa || p.mma_b0[q] + p.mma_n[q] > p.sb ||
+            p.mma_a[q] + p.mma_b0[q] + p.mma_n[q] > p.nslots)
+            return fail(RSTSR_ERR_RUNTIME, "MMA list outside the slices or level slots");
+    if ((reinterpret_cast<uintptr_t>(p.a_stack) & 15) || (reinterpret_cast<uintptr_t>(p.b_stack) & 15))
+        return fail(RSTSR_ERR_RUNTIME, "operand stacks not 16-byte aligned");
     p.a_tile_bytes = (uint32_t)(kTcBM * kt * 2);
     p.b_tile_bytes = (uint32_t)(BN * kt * 2);
     p.stage_bytes = (uint32_t)p.sa * p.a_tile_bytes + (uint32_t)p.sb * p.b_tile_bytes;
-    const size_t budget = 232448 - 1024 - 256;
+    const size_t budget = kTcSmemMax - 1024 - kTcSmemTail;
     p.stages = (int)std::min<size_t>(kTcMaxStages, budget / p.stage_bytes);
     if (p.stages < 1) return fail(RSTSR_ERR_UNIMPLEMENTED, "too many slices for one pipeline stage");
     int64_t ntiles;
@@ -104,18 +67,10 @@ int launch_tc_gemm(rstsr_ctx* ctx, int kt, const void* a_slices, const void* b_s
     }
     if (ntiles == 0) return RSTSR_OK;
     if (ntiles > INT32_MAX) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "too many output tiles");
-    const int total = std::max(k_tiles_total, 1);
-    const int chunk = k_chunk_tiles > 0 ? k_chunk_tiles : total;
-    const int accumulate0 = p.accumulate;
-    for (int k0 = 0; k0 < total; k0 += chunk) {
-        p.kt_begin = k0;
-        p.kt_count = std::min(chunk, k_tiles_total - k0);
-        p.accumulate = k0 == 0 ? accumulate0 : 1;
-        s = BN == 128 ? launch_bn<128>(ctx, kt, ma, mb, p, (unsigned)ntiles)
-                      : launch_bn<96>(ctx, kt, ma, mb, p, (unsigned)ntiles);
-        if (s) return s;
-    }
-    return RSTSR_OK;
+    p.ntiles = (int32_t)ntiles;
+    p.k_tiles = std::max(k_tiles_total, 1);
+    p.chunk_tiles = k_chunk_tiles > 0 ? k_chunk_tiles : p.k_tiles;
+    return p.out_f64 ? launch_out<true>(ctx, kt, p, (unsigned)ntiles) : launch_out<false>(ctx, kt, p, (unsigned)ntiles);
 }
 
 }  // namespace rstsr
