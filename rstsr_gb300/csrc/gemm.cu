@@ -300,14 +300,15 @@ static int gemm_batch(rstsr_ctx* ctx, rstsr_dtype t, const std::vector<GemmProbl
     std::vector<SplitItem> ai, bi;
     std::map<std::tuple<const void*, int64_t, int64_t, int64_t, int64_t>, int> amap, bmap;
     int rows_a = 0, rows_b = 0;
-    auto item = [](std::vector<SplitItem>& v, decltype(amap)& m, int& rows, const void* p, int64_t sr, int64_t sk,
-                   int64_t R, int64_t K) {
+    // items start on the tile layouts' row units: 8-row groups (A), 64-row blocks (B)
+    auto item = [](std::vector<SplitItem>& v, decltype(amap)& m, int& rows, int unit, const void* p, int64_t sr,
+                   int64_t sk, int64_t R, int64_t K) {
         auto key = std::make_tuple(p, sr, sk, R, K);
         auto it = m.find(key);
         if (it != m.end()) return it->second;
         const int idx = (int)v.size();
         v.push_back(SplitItem{p, sr, sk, (int32_t)R, (int32_t)K, rows});
-        rows += (int)((R + 7) / 8 * 8);  // items start on 8-row groups of the tile layout
+        rows += (int)((R + unit - 1) / unit * unit);
         m.emplace(key, idx);
         return idx;
     };
@@ -316,8 +317,8 @@ static int gemm_batch(rstsr_ctx* ctx, rstsr_dtype t, const std::vector<GemmProbl
         if (r.M > INT32_MAX / 8 || r.N > INT32_MAX / 8 || r.K > INT32_MAX / 2)
             return fail(RSTSR_ERR_UNIMPLEMENTED, "matrix too large for the split GEMM");
         SplitProblem sp;
-        sp.ia = item(ai, amap, rows_a, r.A, r.a_si, r.a_sk, r.M, r.K);
-        sp.ib = item(bi, bmap, rows_b, r.B, r.b_sj, r.b_sk, r.N, r.K);  // B^T view [N, K]
+        sp.ia = item(ai, amap, rows_a, 8, r.A, r.a_si, r.a_sk, r.M, r.K);
+        sp.ib = item(bi, bmap, rows_b, 64, r.B, r.b_sj, r.b_sk, r.N, r.K);  // B^T view [N, K]
         sp.M = r.M;
         sp.N = r.N;
         sp.K = r.K;

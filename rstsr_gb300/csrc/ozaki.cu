@@ -155,48 +155,52 @@ __global__ void __launch_bounds__(256) row_stats_kernel(const SegPair segs, unsi
 // fixed-point integer Y = y 2^63 (|Y| < 2^63; bits below 2^-63 of the row
 // maximum are dropped), then balanced base-128 digits from the top,
 // d_s = round(Y / 2^(56 - 7s)) with Y reduced by each digit, so that
-// |d_0| <= 128 and |d_s| <= 64 after it. Slice s is stored as d_s 2^(-7s),
-// exact in bf16. Non-finite x puts itself in slice 0 and zeros after it.
-__device__ __forceinline__ void ozaki_digits(double x, int e_r, int S, __nv_bfloat16* out, size_t plane) {
+// |d_0| <= 128 and |d_s| <= 64 after it. Slice s is d_s 2^(-7s), exact in
+// bf16. Non-finite x puts itself in slice 0 and zeros after it.
+constexpr int kMaxSlices = 8;
+
+__device__ __forceinline__ void ozaki_digits(double x, int e_r, int S, __nv_bfloat16 (&v)[kMaxSlices]) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(x);
     const int E = (int)((u >> 52) & 0x7FF);
     if (E == 0x7FF) {
         const uint32_t nan = (u & 0xFFFFFFFFFFFFFull) ? 0x7FC00000u : 0x7F800000u;
-        out[0] = __float2bfloat16_rn(__uint_as_float((uint32_t)(u >> 32) & 0x80000000u | nan));
-        for (int s = 1; s < S; ++s) out[s * plane] = __float2bfloat16_rn(0.f);
+        v[0] = __float2bfloat16_rn(__uint_as_float((uint32_t)(u >> 32) & 0x80000000u | nan));
+#pragma unroll
+        for (int s = 1; s < kMaxSlices; ++s) v[s] = __float2bfloat16_rn(0.f);
         return;
     }
     const long long mant = (long long)(E ? (u & 0xFFFFFFFFFFFFFull) | (1ull << 52) : (u & 0xFFFFFFFFFFFFFull));
     const int sh = (E ? E : 1) - 1012 - e_r;  // |x| = mant 2^((E ? E : 1) - 1075) < 2^e_r, so Y < 2^63
     long long Y = sh >= 0 ? mant << sh : (sh > -63 ? mant >> -sh : 0);
     if (u >> 63) Y = -Y;
-    for (int s = 0; s < S; ++s) {
+#pragma unroll
+    for (int s = 0; s < kMaxSlices; ++s) {
+        if (s >= S) break;
         const int k = 56 - 7 * s;
         const long long d = (Y >> k) + ((Y >> (k - 1)) & 1);  // round half up, no overflow
         Y -= d << k;
-        out[s * plane] = __float2bfloat16_rn(__int2float_rn((int)d) * __int_as_float((127 - 7 * s) << 23));
+        v[s] = __float2bfloat16_rn(__int2float_rn((int)d) * __int_as_float((127 - 7 * s) << 23));
     }
 }
 
 // Cut every item into slices, written into the stack of its side in the
-// tensor-core tile layout (tc_tiled_offset with KT = 2^lkt and G row groups:
-// slice s of element (row, k) lies s * G * 8 * KT after slice 0), zero in
-// [K, pitch).
+// tensor-core tile layouts (KT = 2^lkt): A items as tc_offset_a (groups_a row
+// groups, slice stride 8 KT), B items as tc_offset_b (blocks_b 64-row blocks,
+// slice stride 64 KT); with `dual` (a symmetric product, B = A) the A items
+// are written in both layouts. Zero in [K, pitch).
 // MODE 0: Ozaki integer slices (ozaki_digits); the k-tile-0 blocks also store
 //         the row exponents e_r (max_r < 2^e_r) from the row maxima.
 // MODE 1: f32 three-term split hi / mid / lo.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitch, int S, int lkt, int groups_a,
-                                                    int groups_b, const unsigned long long* __restrict__ maxbits,
+                                                    int blocks_b, int dual,
+                                                    const unsigned long long* __restrict__ maxbits,
                                                     int32_t* __restrict__ exps, __nv_bfloat16* __restrict__ out_a,
                                                     __nv_bfloat16* __restrict__ out_b) {
     bool is_b;
     const SplitItem it = pair_item(segs, blockIdx.z, is_b);
     const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
     if (r0 >= it.R || k0 >= pitch) return;  // uniform per block
-    const int G = is_b ? groups_b : groups_a;
-    const size_t plane = (size_t)G << (3 + lkt);
-    __nv_bfloat16* out = is_b ? out_b : out_a;
     const int base = (is_b ? segs.rows_a : 0) + it.row0;  // statistics row of r = 0
     __shared__ T tile[32][33];
     const T* X = (const T*)it.ptr;
@@ -212,32 +216,43 @@ __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitc
         tile[rr][kk] = v;
     }
     __syncthreads();
+    const int KT = 1 << lkt;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const int rr = ty + 8 * j;
         const int r = r0 + rr, k = k0 + tx;
         if (r >= it.R || k >= pitch) continue;
-        const int row = it.row0 + r;
-        const size_t o = ((((size_t)(k >> lkt) * S) * G + (size_t)(row >> 3)) << (3 + lkt)) +
-                         (size_t)((((k & ((1 << lkt) - 1)) >> 3) << 6) + ((row & 7) << 3) + (k & 7));
+        __nv_bfloat16 v[kMaxSlices];
         if (k >= it.K) {
-            for (int s = 0; s < S; ++s) out[s * plane + o] = __float2bfloat16_rn(0.f);
-            continue;
-        }
-        if constexpr (MODE == 0) {
+#pragma unroll
+            for (int s = 0; s < kMaxSlices; ++s) v[s] = __float2bfloat16_rn(0.f);
+        } else if constexpr (MODE == 0) {
             const int e_r = exp_above(maxbits[base + r]);
             if (k == 0) exps[base + r] = e_r;
-            ozaki_digits((double)tile[rr][tx], e_r, S, out + o, plane);
+            ozaki_digits((double)tile[rr][tx], e_r, S, v);
         } else {
             const float x = (float)tile[rr][tx];
-            const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-            const float r1 = x - __bfloat162float(hi);
-            const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
-            const float r2 = r1 - __bfloat162float(mid);
-            const __nv_bfloat16 lo = __float2bfloat16_rn(r2);
-            out[o] = hi;
-            if (S > 1) out[plane + o] = mid;
-            if (S > 2) out[2 * plane + o] = lo;
+            v[0] = __float2bfloat16_rn(x);
+            const float r1 = x - __bfloat162float(v[0]);
+            v[1] = __float2bfloat16_rn(r1);
+            v[2] = __float2bfloat16_rn(r1 - __bfloat162float(v[1]));
+        }
+        const int row = it.row0 + r;
+        const size_t kt = (size_t)(k >> lkt);
+        const size_t inner = (size_t)((((k & (KT - 1)) >> 3) << 6) + ((row & 7) << 3) + (k & 7));
+        if (!is_b) {
+            __nv_bfloat16* o = out_a + (((kt * groups_a + (size_t)(row >> 3)) * S) << (3 + lkt)) + inner;
+#pragma unroll
+            for (int s = 0; s < kMaxSlices; ++s)
+                if (s < S) o[(size_t)s << (3 + lkt)] = v[s];
+        }
+        if (is_b || dual) {
+            __nv_bfloat16* o =
+                out_b + ((((kt * blocks_b + (size_t)(row >> 6)) * S) * 8 + (size_t)((row >> 3) & 7)) << (3 + lkt)) +
+                inner;
+#pragma unroll
+            for (int s = 0; s < kMaxSlices; ++s)
+                if (s < S) o[(size_t)s << (6 + lkt)] = v[s];
         }
     }
 }
@@ -380,23 +395,26 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     const int kt = kt_for_stages(S, BN);
     const int lkt = kt == 64 ? 6 : kt == 32 ? 5 : 4;
     const int pitch = (maxk + kt - 1) / kt * kt;
-    // slice stacks in the tile layout; row groups past the last row cover the
-    // rows a 128-row A tile or 64-row B tile may read beyond it
-    const int groups_a = (rows_a + 7) / 8 + kTcBM / 8, groups_b = (rows_b + 7) / 8 + kTcBM / 8;
-    const size_t stack_a = (size_t)S * pitch * groups_a * 8, stack_b = b_items.empty() ? 0 : (size_t)S * pitch * groups_b * 8;
+    // slice stacks in the tile layouts; the row groups / blocks past the last
+    // row cover what a 128-row A tile or 64-row B tile reads beyond it. A
+    // symmetric product (B = A) keeps its A items in both layouts.
+    const bool dual = b_items.empty();
+    const int rows_bl = dual ? rows_a : rows_b;
+    const int groups_a = (rows_a + 7) / 8 + kTcBM / 8, blocks_b = (rows_bl + 63) / 64 + 1;
+    const size_t stack_a = (size_t)S * pitch * groups_a * 8, stack_b = (size_t)S * pitch * blocks_b * 64;
     void* sl = nullptr;
     if ((s = scratch_alloc(ctx, (stack_a + stack_b) * 2, &sl))) return cleanup(), s;
     owned.push_back(sl);
     auto* as = (__nv_bfloat16*)sl;
-    auto* bs = b_items.empty() ? as : as + stack_a;
+    auto* bs = as + stack_a;
     {
         const dim3 g = grid_for(a_items, b_items, pitch);
         if (f64)
-            split_kernel<double, 0>
-                <<<g, 256, 0, ctx->stream>>>(segs, pitch, S, lkt, groups_a, groups_b, maxbits, exps, as, bs);
+            split_kernel<double, 0><<<g, 256, 0, ctx->stream>>>(segs, pitch, S, lkt, groups_a, blocks_b, dual ? 1 : 0,
+                                                                maxbits, exps, as, bs);
         else
-            split_kernel<float, 1>
-                <<<g, 256, 0, ctx->stream>>>(segs, pitch, S, lkt, groups_a, groups_b, nullptr, nullptr, as, bs);
+            split_kernel<float, 1><<<g, 256, 0, ctx->stream>>>(segs, pitch, S, lkt, groups_a, blocks_b, dual ? 1 : 0,
+                                                               nullptr, nullptr, as, bs);
         if ((s = after_launch(ctx, "split_kernel"))) return cleanup(), s;
     }
     // products and accumulators
@@ -407,7 +425,7 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     p.a_stack = as;
     p.b_stack = bs;
     p.a_groups = groups_a;
-    p.b_groups = b_items.empty() ? groups_a : groups_b;
+    p.b_blocks = blocks_b;
     // products A_a B_b with a + b < L, level a + b in TMEM slot a + b: for each
     // A slice, its B slices 0 .. L-1-a in runs of up to four per MMA
     int nm = 0;

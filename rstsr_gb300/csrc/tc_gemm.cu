@@ -59,8 +59,18 @@ int launch_tc_gemm(rstsr_ctx* ctx, int kt, TcGemmParams p, int k_tiles_total, in
         if (p.group_m <= 0) p.group_m = 8;
         if (p.symmetric) {
             if (p.M != p.N) return fail(RSTSR_ERR_INVALID_LAYOUT, "symmetric product must be square");
+            // bands of at least 16 row tiles (2048 rows), at most kTcMaxBands of them
+            p.band_rows = std::max(16, (p.tiles_m + kTcMaxBands - 1) / kTcMaxBands);
+            p.nbands = (p.tiles_m + p.band_rows - 1) / p.band_rows;
             ntiles = 0;
-            for (int j = 0; j < p.tiles_n; ++j) ntiles += p.tiles_m - (j * BN) / kTcBM;
+            for (int g = 0; g < p.nbands; ++g) {
+                if (ntiles > INT32_MAX) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "too many output tiles");
+                p.band_first[g] = (int32_t)ntiles;
+                const int bs = g * p.band_rows, be = std::min(bs + p.band_rows, p.tiles_m);
+                const int jmax = std::min(2 * be, p.tiles_n);
+                for (int j = 0; j < jmax; ++j) ntiles += be - std::max(bs, j >> 1);
+            }
+            p.band_first[p.nbands] = (int32_t)std::min<int64_t>(ntiles, INT32_MAX);
         } else {
             ntiles = (int64_t)p.tiles_m * p.tiles_n;
         }
@@ -68,6 +78,7 @@ int launch_tc_gemm(rstsr_ctx* ctx, int kt, TcGemmParams p, int k_tiles_total, in
     if (ntiles == 0) return RSTSR_OK;
     if (ntiles > INT32_MAX) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "too many output tiles");
     p.ntiles = (int32_t)ntiles;
+    p.nbuf = p.nslots * BN <= (int)kTcBufCols ? 2 : 1;
     p.k_tiles = std::max(k_tiles_total, 1);
     p.chunk_tiles = k_chunk_tiles > 0 ? k_chunk_tiles : p.k_tiles;
     return p.out_f64 ? launch_out<true>(ctx, kt, p, (unsigned)ntiles) : launch_out<false>(ctx, kt, p, (unsigned)ntiles);

@@ -2,13 +2,15 @@
 //
 // Work unit: a 128 x 64 output tile and one K chunk of it. The operands are
 // stacks of bf16 "slices" written by the split kernel directly in the tensor
-// cores' shared-memory image (tc_tiled_offset): K tiles of width KT, each
-// holding per slice the 8-row groups of all rows as core matrices (8 rows x
-// 16 bytes, K-major, no swizzle). The rows of one tile of one slice are then a
-// single contiguous block of 128 x KT (A) or 64 x KT (B) elements, fetched by
-// one bulk copy: large sequential L2 requests instead of one 2 KT-byte
-// request per row. Per K tile, one pipeline stage holds every slice of the A
-// and B tiles, the B slices stacked along N. The products A_a * B_b accumulate in FP32 TMEM
+// cores' shared-memory image: core matrices of 8 rows x 16 bytes (K-major, no
+// swizzle), ordered so that every slice of one operand tile in one K tile of
+// width KT is a single contiguous block (tc_offset_a: row group, then slice;
+// tc_offset_b: 64-row block, then slice, then row group). A pipeline stage is
+// then two bulk copies. Measured on GB300: the copy count, not the bytes,
+// bounds a SM's intake (16 B per cycle with 2 KB copies, 50 with one 43 KB
+// copy), and a stage of this kernel needs about 46 B per cycle to keep the
+// tensor cores busy. In shared memory the B slices are stacked along N. The
+// products A_a * B_b accumulate in FP32 TMEM
 // "level slots": slot l (columns 64 l .. 64 l + 63) sums every product with
 // a + b = l. Since slot a + b follows slot a + b - 1, the products of one A
 // slice with B slices b0 .. b0 + n - 1 are a single tcgen05.mma with N = 64 n
@@ -31,11 +33,13 @@
 // list {problem, tile row, tile column}.
 //
 // Persistent: one CTA per SM walks tiles blockIdx.x, + gridDim.x, ... Roles
-// (320 threads): warp 0 streams TMA loads through a ring of stages, warp 1
-// owns TMEM and issues tcgen05.mma from one thread (descriptors precomputed in
-// registers: an MMA loop that reads its product list from memory issued one
-// MMA per ~90 cycles on GB300, slower than the MMAs), warps 2-9 are the
-// epilogue (warp w reads TMEM lanes 32*(w%4)..+31, columns of half (w-2)/4).
+// (576 threads): warp 0 streams bulk copies through a ring of stages, warp 1
+// owns TMEM and issues tcgen05.mma from one thread, warps 2-17 are the
+// epilogue (warp w reads TMEM lanes 32*(w%4)..+31 and 16 columns of part
+// (w-2)/4). Measured
+// on GB300 for 7 slices: the MMAs of a 16-wide K step take 921 cycles alone;
+// behind the stage barrier wait of one issuing thread they take about 1150
+// (the MMA queue is shallower than the wait).
 // The epilogue copies a unit's slots into registers, zeroes them (the MMAs
 // always accumulate: a stacked MMA cannot start some of its slots and add to
 // others) and releases TMEM, so that the next unit's MMAs run while it
@@ -50,16 +54,23 @@ namespace rstsr {
 
 constexpr int kTcBM = 128;
 // Tile width = level slot width: eight slots of 64 columns fill the 512 TMEM
-// columns, and 32 columns per epilogue warp fit its registers (three warps per
-// scheduler leave 168 registers a thread).
+// columns.
 constexpr int kTcBN = 64;
-constexpr int kTcEpiWarps = 8;
-constexpr int kTcThreads = 64 + 32 * kTcEpiWarps;
+// Sixteen epilogue warps, four per TMEM lane quadrant with 16 columns each:
+// draining TMEM is latency-bound, and the MMAs wait for it at every unit of a
+// single-buffered problem (five warps per scheduler leave 96 registers a
+// thread).
+constexpr int kTcEpiWarps = 16;
+constexpr int kTcEpiCols = kTcBN * 4 / kTcEpiWarps;
+constexpr int kTcEpiWarp0 = 2;    // first epilogue warp
+constexpr int kTcThreads = 32 * (kTcEpiWarp0 + kTcEpiWarps);
 constexpr int kTcMaxStages = 8;
 constexpr int kTcMaxSlots = 8;
-constexpr int kTcMaxMma = 16;      // MMA instructions per 16-wide K step
+constexpr int kTcMaxMma = 12;      // MMA instructions per 16-wide K step (11 for 8 slices)
 constexpr int kTcMaxStack = 4;     // B slices stacked in one MMA (N <= 256)
 constexpr uint32_t kTcTmemCols = 512;
+constexpr int kTcMaxBands = 64;    // row bands of the symmetric tile order
+constexpr uint32_t kTcBufCols = 256;  // second accumulator buffer (when the slots fit twice)
 
 // error codes written to p.err
 constexpr int kTcErrProducerWait = 1;
@@ -79,19 +90,30 @@ struct TcProblem {
     double alpha, beta;
 };
 
-// Element (slice s, row, k) of an operand stack of S slices whose rows are
-// padded to 8 * G: K tile kt = k / KT holds, per slice, G row groups of KT / 8
-// core matrices of 8 x 8 elements.
-__host__ __device__ __forceinline__ size_t tc_tiled_offset(int S, int G, int KT, int s, int row, int k) {
+// Element (slice s, row, k) of the A operand stack (S slices, G row groups):
+// K tile kt = k / KT holds, per row group, the S slices' KT / 8 core matrices
+// of 8 x 8 elements. Slice s + 1 lies 8 KT elements after slice s; a 128-row
+// tile is 16 consecutive row groups.
+__host__ __device__ __forceinline__ size_t tc_offset_a(int S, int G, int KT, int s, int row, int k) {
     const int kt = k / KT, kk = k % KT;
-    return (((size_t)kt * S + s) * G + (size_t)(row >> 3)) * (size_t)(8 * KT) + (size_t)((kk >> 3) * 64) +
+    return (((size_t)kt * G + (size_t)(row >> 3)) * S + s) * (size_t)(8 * KT) + (size_t)((kk >> 3) * 64) +
            (size_t)((row & 7) * 8 + (k & 7));
 }
 
+// Element (slice s, row, k) of the B operand stack (S slices, NB blocks of 64
+// rows): K tile kt holds, per 64-row block, the S slices' 8 row groups. Slice
+// s + 1 lies 64 KT elements after slice s.
+__host__ __device__ __forceinline__ size_t tc_offset_b(int S, int NB, int KT, int s, int row, int k) {
+    const int kt = k / KT, kk = k % KT;
+    return ((((size_t)kt * NB + (size_t)(row >> 6)) * S + s) * 8 + (size_t)((row >> 3) & 7)) * (size_t)(8 * KT) +
+           (size_t)((kk >> 3) * 64) + (size_t)((row & 7) * 8 + (k & 7));
+}
+
 struct TcGemmParams {
-    const __nv_bfloat16* a_stack;  // operand stacks (tc_tiled_offset layout)
+    const __nv_bfloat16* a_stack;  // operand stacks (tc_offset_a / tc_offset_b layouts)
     const __nv_bfloat16* b_stack;
-    int32_t a_groups, b_groups;  // G of each stack
+    int32_t a_groups;            // G: 8-row groups of the A stack
+    int32_t b_blocks;            // NB: 64-row blocks of the B stack
     int32_t M, N;                // single-problem mode: output extent
     int32_t k_tiles;             // single-problem mode: K tiles
     int32_t chunk_tiles;         // K tiles summed in TMEM before the epilogue adds them to C
@@ -117,27 +139,46 @@ struct TcGemmParams {
     int32_t symmetric;           // lower triangle only (row >= col), mirrored
     int32_t tiles_m, tiles_n;
     int32_t group_m;             // raster swizzle: tiles grouped along M
+    int32_t nbuf;                // TMEM accumulator buffers (2 when 2 * nslots * BN <= 512)
+    // symmetric order: bands of band_rows row tiles; band g's first tile
+    int32_t band_rows, nbands;
+    int32_t band_first[kTcMaxBands + 1];
     // grouped mode (tiles != null): tile t is tiles[t] = {problem, tm, tn, 0}
     const int4* tiles;
     const TcProblem* problems;
     int* err;
 };
 
-// Tile of a single-problem launch. Symmetric problems enumerate, column tile
-// by column tile, the tiles that hold at least one element with row >= col.
+// Tile of a single-problem launch. Symmetric problems enumerate the tiles that
+// hold an element with row >= col (row tile tm, column tile j with j / 2 <=
+// tm) band by band: band g is row tiles [g R, g R + R) (R = band_rows), its
+// columns left to right, each column's rows top to bottom. A band's A rows
+// stay in L2 while its columns stream by; a plain column-by-column order
+// re-reads all of A from HBM once per column. Other problems use a grouped
+// raster: group_m row tiles share each B tile.
 template <int BN>
 __device__ __forceinline__ void tc_tile_coords(const TcGemmParams& p, int bid, int& tm, int& tn) {
+    static_assert(2 * BN == kTcBM, "column tile j first meets the lower triangle at row tile j / 2");
     if (p.symmetric) {
-        int rem = bid;
-        for (int j = 0; j < p.tiles_n; ++j) {
-            const int first = (j * BN) / kTcBM;
-            const int cnt = p.tiles_m - first;
-            if (rem < cnt) {
-                tm = first + rem;
+        int g = 0;
+        while (g + 1 < p.nbands && p.band_first[g + 1] <= bid) ++g;
+        const int bs = g * p.band_rows, be = min(bs + p.band_rows, p.tiles_m), h = be - bs;
+        const int jmax = min(2 * be, p.tiles_n), nf = min(2 * bs + 2, jmax);
+        int t = bid - p.band_first[g];
+        if (t < nf * h) {
+            tn = t / h;
+            tm = bs + t % h;
+            return;
+        }
+        t -= nf * h;
+        for (int j = nf; j < jmax; ++j) {
+            const int first = j >> 1, cnt = be - first;
+            if (t < cnt) {
+                tm = first + t;
                 tn = j;
                 return;
             }
-            rem -= cnt;
+            t -= cnt;
         }
         tm = tn = 0;
         return;
@@ -199,21 +240,9 @@ __device__ __forceinline__ void tc_resolve(const TcGemmParams& p, int t, TcUnit&
 }
 
 // ---- epilogue arithmetic. GB300 runs FP64 instructions at a small fraction
-// of its FP32 and integer rates, so the f64 epilogue adds the FP32
-// accumulators as 64-bit fixed-point integers and builds the double from its
+// of its FP32 and integer rates, so the f64 epilogue adds the FP32 level slots
+// as 64-bit fixed-point integers (2^-37 units) and builds the double from its
 // bits; the f32 epilogue stays in FP32 with an error-free two-sum.
-
-// trunc(f 2^37) for an accumulator f given as bits. The accumulators of one K
-// chunk of at most 1024 stay below 2^24.1 in magnitude, so the sum of all of
-// them stays below 2^62; the truncation error is below 2^-37 per accumulator.
-__device__ __forceinline__ long long acc_fixed37(uint32_t u) {
-    const int e = (int)((u >> 23) & 0xFF);
-    const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u);
-    const int sh = e - 113;  // f 2^37 = m 2^(e - 150 + 37)
-    long long v = sh >= 0 ? m << min(sh, 39) : m >> min(-sh, 63);
-    if (e == 0) v = 0;
-    return (u >> 31) ? -v : v;
-}
 
 // v 2^e rounded to the nearest double (ties to even) into *out; false when the
 // result is subnormal or overflows (left to epilogue_rare).
@@ -244,25 +273,22 @@ static __device__ __noinline__ double epilogue_rare(long long v, int e, int spec
 
 // Zero this warp's columns of every level slot, then tell the MMA thread that
 // TMEM is free for the next unit.
-template <int BN>
+template <int BN, int EC>
 __device__ __forceinline__ void tc_zero_release(const TcGemmParams& p, uint32_t tbase, uint64_t* tmem_empty,
                                                 int lane) {
-    for (int a = 0; a < p.nslots; ++a) {
-#pragma unroll
-        for (int j0 = 0; j0 < BN / 2; j0 += 16) tc::tmem_st_zero_x16(tbase + (uint32_t)(a * BN + j0));
-    }
+    static_assert(EC == 16, "one 16-column store per slot");
+    for (int a = 0; a < p.nslots; ++a) tc::tmem_st_zero_x16(tbase + (uint32_t)(a * BN));
     tc::tmem_st_wait();
     tc::tc_fence_before();
     __syncwarp();
     if (lane == 0) tc::mbar_arrive(tmem_empty);
 }
 
-// Load this warp's EC (= 32) columns of level slot a.
+// Load this warp's EC (= 16) columns of level slot a.
 template <int BN, int EC>
 __device__ __forceinline__ void tc_load_slot(uint32_t tbase, int a, uint32_t (&r)[EC]) {
-    static_assert(EC == 32, "two 16-column loads per slot");
+    static_assert(EC == 16, "one 16-column load per slot");
     tc::tmem_ld_32x32b_x16(tbase + (uint32_t)(a * BN), r);
-    tc::tmem_ld_32x32b_x16(tbase + (uint32_t)(a * BN + 16), r + 16);
     tc::tmem_ld_wait();
 }
 
@@ -272,26 +298,27 @@ __device__ __forceinline__ void tc_epilogue_f64(const TcGemmParams& p, const TcU
                                                 uint64_t* tmem_empty, int64_t row, int64_t col0, int mode,
                                                 int lane, int* colexp) {
     long long fx[EC];
-    unsigned long long m_nan = 0, m_pinf = 0, m_ninf = 0;
+    float fs[EC];  // FP32 sum of the slots: non-finite iff a slot is (inf / NaN inputs)
 #pragma unroll
-    for (int i = 0; i < EC; ++i) fx[i] = 0;
+    for (int i = 0; i < EC; ++i) fx[i] = 0, fs[i] = 0.f;
     for (int a = 0; a < p.nslots; ++a) {
         uint32_t r[EC];
         tc_load_slot<BN, EC>(tbase, a, r);
+        // slot a as fixed point at 2^-37: levels 0-3 hold integers times
+        // 2^(-7a) below 2^24.7 (K chunk <= 1024, digits |d_0| <= 128, |d_s| <=
+        // 64), converted exactly; higher levels are below 2^-3, converted at
+        // 2^-34 (error below 2^-35 a slot)
+        const float sc = __int_as_float((127 + (a < 4 ? 7 * a : 34)) << 23);
+        const int sh = a < 4 ? 37 - 7 * a : 3;
 #pragma unroll
         for (int i = 0; i < EC; ++i) {
-            const uint32_t x = r[i];
-            fx[i] += acc_fixed37(x);
-            if ((x & 0x7F800000u) == 0x7F800000u) {
-                const unsigned long long bit = 1ull << i;
-                if (x & 0x7FFFFFu) m_nan |= bit;
-                else if (x >> 31) m_ninf |= bit;
-                else m_pinf |= bit;
-            }
+            const float v = __uint_as_float(r[i]);
+            fx[i] += (long long)__float2int_rn(v * sc) << sh;
+            fs[i] += v;
         }
     }
     // the slots are in registers: zero them for the next unit's MMAs
-    tc_zero_release<BN>(p, tbase, tmem_empty, lane);
+    tc_zero_release<BN, EC>(p, tbase, tmem_empty, lane);
     // column exponents of this warp's columns, staged in its shared-memory slot
     for (int j = lane; j < EC; j += 32) {
         const int64_t col = col0 + j;
@@ -300,30 +327,37 @@ __device__ __forceinline__ void tc_epilogue_f64(const TcGemmParams& p, const TcU
     __syncwarp();
     if (row >= u.M) return;
     const int rexp = (u.row_exp ? u.row_exp[row] : 0) + p.exp_bias - 37;
-    const bool scale = u.alpha != 1.0;
-    double* Cd = reinterpret_cast<double*>(u.C);
-    const unsigned long long m_any = m_nan | m_pinf | m_ninf;
+    const int ncol = (int)(u.N - col0 < (int64_t)EC ? u.N - col0 : (int64_t)EC);
+    // the products as doubles, in place of their fixed-point sums
 #pragma unroll
     for (int i = 0; i < EC; ++i) {
-        const int64_t col = col0 + i;
-        if (col >= u.N) break;
-        if (u.symmetric && col > row) continue;  // upper triangle: written by the mirror
         const int e = rexp + colexp[i];
         double x;
-        const unsigned long long bit = 1ull << i;
-        if (!fixed_to_double(fx[i], e, &x) || (m_any & bit)) {
-            const int special = (m_nan & bit) || ((m_pinf & bit) && (m_ninf & bit)) ? 2
-                                : (m_pinf & bit)                                    ? 1
-                                : (m_ninf & bit)                                    ? -1
-                                                                                    : 0;
-            x = epilogue_rare(fx[i], e, special);
+        if (!fixed_to_double(fx[i], e, &x) || !isfinite(fs[i]))
+            x = epilogue_rare(fx[i], e, isnan(fs[i]) ? 2 : isinf(fs[i]) ? (fs[i] > 0 ? 1 : -1) : 0);
+        if (u.alpha != 1.0) x *= u.alpha;
+        fx[i] = __double_as_longlong(x);
+    }
+    double* Cd = reinterpret_cast<double*>(u.C) + row * u.ldc;
+    if (mode != 0) {
+        // C of the later K chunks / beta C: all loads first (independent)
+        double c[EC];
+#pragma unroll
+        for (int i = 0; i < EC; ++i) c[i] = i < ncol ? Cd[col0 + i] : 0.0;
+#pragma unroll
+        for (int i = 0; i < EC; ++i) {
+            const double x = __longlong_as_double(fx[i]);
+            fx[i] = __double_as_longlong(mode == 1 ? x + c[i] : fma(u.beta, c[i], x));
         }
-        if (scale) x *= u.alpha;
-        double* dst = Cd + row * u.ldc + col;
-        if (mode == 1) x += *dst;
-        else if (mode == 2) x = fma(u.beta, *dst, x);
-        *dst = x;
-        if (u.symmetric && col != row) Cd[col * u.ldc + row] = x;
+    }
+#pragma unroll
+    for (int i = 0; i < EC; ++i) {
+        if (i >= ncol) break;
+        const int64_t col = col0 + i;
+        if (u.symmetric && col > row) continue;  // upper triangle: written by the mirror
+        const double x = __longlong_as_double(fx[i]);
+        Cd[col0 + i] = x;
+        if (u.symmetric && col != row) reinterpret_cast<double*>(u.C)[col * u.ldc + row] = x;
     }
 }
 
@@ -344,50 +378,55 @@ __device__ __forceinline__ void tc_epilogue_f32(const TcGemmParams& p, const TcU
             else t[i] += x;
         }
     }
-    tc_zero_release<BN>(p, tbase, tmem_empty, lane);
+    tc_zero_release<BN, EC>(p, tbase, tmem_empty, lane);
     if (row >= u.M) return;
     const float af = (float)u.alpha, bf = (float)u.beta;
-    float* Cf = reinterpret_cast<float*>(u.C);
+    float* Cf = reinterpret_cast<float*>(u.C) + row * u.ldc;
+    const int ncol = (int)(u.N - col0 < (int64_t)EC ? u.N - col0 : (int64_t)EC);
+    // C of the later K chunks / beta C: all loads first (independent), then compute and store
+    float c[EC];
+    if (mode != 0) {
+#pragma unroll
+        for (int i = 0; i < EC; ++i) c[i] = i < ncol ? Cf[col0 + i] : 0.f;
+    }
 #pragma unroll
     for (int i = 0; i < EC; ++i) {
+        if (i >= ncol) break;
         const int64_t col = col0 + i;
-        if (col >= u.N) break;
         if (u.symmetric && col > row) continue;
-        float* dst = Cf + row * u.ldc + col;
         const float ph = af * s0[i], pl = fmaf(af, s0[i], -ph);
         float ch = 0.f, cl = 0.f;
         if (mode == 1) {
-            ch = *dst;
+            ch = c[i];
         } else if (mode == 2) {
-            const float c = *dst;
-            ch = bf * c;
-            cl = fmaf(bf, c, -ch);
+            ch = bf * c[i];
+            cl = fmaf(bf, c[i], -ch);
         }
         const float sh = ph + ch, bb = sh - ph;
         const float se = (ph - (sh - bb)) + (ch - bb);
         const float y = sh + (se + pl + cl + af * t[i]);
-        *dst = y;
-        if (u.symmetric && col != row) Cf[col * u.ldc + row] = y;
+        Cf[col0 + i] = y;
+        if (u.symmetric && col != row) reinterpret_cast<float*>(u.C)[col * u.ldc + row] = y;
     }
 }
 
 // Dynamic shared memory: the stages, then kTcSmemTail bytes of barriers,
 // TMEM slot, abort flag (256 bytes) and the epilogue warps' column-exponent
-// slots (64 ints each), plus 1024 bytes of alignment slack in front.
-constexpr size_t kTcSmemTail = 256 + kTcEpiWarps * 64 * 4;
+// slots (kTcEpiCols ints each), plus 1024 bytes of alignment slack in front.
+constexpr size_t kTcSmemTail = 256 + kTcEpiWarps * kTcEpiCols * 4;
 constexpr size_t kTcSmemMax = 232448;
 
 template <int KT, int BN, bool F64>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmParams p) {
-    constexpr int EC = BN / 2;  // columns per epilogue warp
-    static_assert(EC <= 64, "column masks and exponent slots hold 64 columns");
+    constexpr int EC = kTcEpiCols;  // columns per epilogue warp
+    static_assert(BN == kTcBN, "one tile width");
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + (size_t)p.stages * p.stage_bytes);
     uint64_t* empty = full + kTcMaxStages;
-    uint64_t* accum_full = empty + kTcMaxStages;
-    uint64_t* tmem_empty = accum_full + 1;
-    uint64_t* mma_done = tmem_empty + 1;
+    uint64_t* accum_full = empty + kTcMaxStages;  // per TMEM buffer
+    uint64_t* tmem_empty = accum_full + 2;        // per TMEM buffer
+    uint64_t* mma_done = tmem_empty + 2;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* colexp_all = reinterpret_cast<int*>(reinterpret_cast<uint8_t*>(full) + 256);
@@ -400,8 +439,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 1);
         }
-        tc::mbar_init(accum_full, 1);
-        tc::mbar_init(tmem_empty, kTcEpiWarps);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&accum_full[b], 1);
+            tc::mbar_init(&tmem_empty[b], kTcEpiWarps);
+        }
         tc::mbar_init(mma_done, 1);
         *abort_flag = 0;
         tc::fence_barrier_init();
@@ -431,16 +472,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
                     }
                     uint8_t* st = smem + (size_t)s * p.stage_bytes;
                     tc::mbar_arrive_expect_tx(&full[s], p.stage_bytes);
-                    const int ga = (u.a_row0 + u.tm * kTcBM) >> 3, gb = (u.b_row0 + u.tn * BN) >> 3;
-                    for (int a = 0; a < p.sa; ++a)
-                        tc::bulk_load(st + (size_t)a * p.a_tile_bytes,
-                                      p.a_stack + (((size_t)kt * p.sa + a) * p.a_groups + ga) * (8 * KT),
-                                      p.a_tile_bytes, &full[s]);
-                    uint8_t* sb = st + (size_t)p.sa * p.a_tile_bytes;
-                    for (int b = 0; b < p.sb; ++b)
-                        tc::bulk_load(sb + (size_t)b * p.b_tile_bytes,
-                                      p.b_stack + (((size_t)kt * p.sb + b) * p.b_groups + gb) * (8 * KT),
-                                      p.b_tile_bytes, &full[s]);
+                    // A: 16 row groups x S slices; B: one 64-row block x S slices
+                    const int ga = (u.a_row0 + u.tm * kTcBM) >> 3, bb = (u.b_row0 + u.tn * BN) >> 6;
+                    tc::bulk_load(st, p.a_stack + ((size_t)kt * p.a_groups + ga) * p.sa * (8 * KT),
+                                  (uint32_t)p.sa * p.a_tile_bytes, &full[s]);
+                    tc::bulk_load(st + (size_t)p.sa * p.a_tile_bytes,
+                                  p.b_stack + ((size_t)kt * p.b_blocks + bb) * p.sb * (64 * KT),
+                                  (uint32_t)p.sb * p.b_tile_bytes, &full[s]);
                     issued = it + 1;
                 }
             }
@@ -454,29 +492,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
         __syncwarp();
     } else if (warp == 1) {
         if (lane == 0) {
-            // the MMA list of one 16-wide K step as descriptor offsets (16-byte
-            // units, relative to the stage), instruction descriptors and TMEM
-            // addresses, kept in registers
-            uint32_t a_off[kTcMaxMma], b_off[kTcMaxMma], idesc[kTcMaxMma], dcol[kTcMaxMma];
+            // the MMA list of one 16-wide K step: stage-relative descriptors
+            // (16-byte units), instruction descriptors and TMEM columns.
+            // Along K, core matrices are 128 bytes apart; along M the A row
+            // groups are S slices apart (A slice a starts a * 16 KT bytes in),
+            // along N the B row groups adjacent (B slice b starts b * BN * 2 KT
+            // bytes after the S A tiles).
+            const uint64_t desc_a = tc::smem_desc_noswizzle(128, (uint32_t)p.sa * 16 * KT);
+            const uint64_t desc_b = tc::smem_desc_noswizzle(128, 16 * KT);
+            const uint32_t b_base = ((uint32_t)p.sa * p.a_tile_bytes) >> 4, b_step = p.b_tile_bytes >> 4;
+            uint32_t pa[kTcMaxMma], pb[kTcMaxMma], pid[kTcMaxMma], pdc[kTcMaxMma];  // low descriptor words
             const int nmma = min(p.nmma, kTcMaxMma);
 #pragma unroll
             for (int q = 0; q < kTcMaxMma; ++q) {
                 const int qq = q < nmma ? q : 0;
-                a_off[q] = ((uint32_t)p.mma_a[qq] * p.a_tile_bytes) >> 4;
-                b_off[q] = ((uint32_t)p.sa * p.a_tile_bytes + (uint32_t)p.mma_b0[qq] * p.b_tile_bytes) >> 4;
-                idesc[q] = tc::idesc_bf16_f32(kTcBM, (uint32_t)BN * p.mma_n[qq]);
-                dcol[q] = tmem_base + (uint32_t)(p.mma_a[qq] + p.mma_b0[qq]) * BN;
+                const uint32_t a = p.mma_a[qq], b0 = p.mma_b0[qq], n = p.mma_n[qq];
+                pa[q] = a * KT;
+                pb[q] = b_base + b0 * b_step;
+                pid[q] = tc::idesc_bf16_f32(kTcBM, BN * n);
+                pdc[q] = tmem_base + (a + b0) * BN;
             }
-            // core matrices: 128 bytes apart along K, 16 KT bytes apart along M/N
-            const uint64_t desc_hi = tc::smem_desc_noswizzle(128, 16 * KT);
             uint32_t it = 0, unit = 0;
             bool stop = false;
             for (int t = blockIdx.x; t < p.ntiles && !stop; t += gridDim.x) {
                 TcUnit u;
                 tc_resolve<BN>(p, t, u);
                 for (int c0 = 0; c0 < u.k_tiles && !stop; c0 += p.chunk_tiles, ++unit) {
-                    // the epilogue has copied out and zeroed the previous unit's slots
-                    if (!tc::mbar_wait(tmem_empty, unit & 1u)) {
+                    // unit u uses TMEM buffer u % nbuf for the (u / nbuf)-th time: the
+                    // epilogue has copied out and zeroed that buffer's previous unit
+                    const uint32_t buf = unit % (uint32_t)p.nbuf, use = unit / (uint32_t)p.nbuf;
+                    if (!tc::mbar_wait(&tmem_empty[buf], use & 1u)) {
                         atomicExch(p.err, kTcErrTmemWait);
                         *abort_flag = 1;
                     }
@@ -485,6 +530,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
                         break;
                     }
                     tc::tc_fence_after();
+                    const uint32_t dbuf = buf * kTcBufCols;
                     const int c1 = min(c0 + p.chunk_tiles, u.k_tiles);
                     for (int kt = c0; kt < c1; ++kt, ++it) {
                         const uint32_t s = it % stages;
@@ -501,18 +547,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
                         const uint32_t st4 = tc::smem_u32(smem + (size_t)s * p.stage_bytes) >> 4;
 #pragma unroll
                         for (int j = 0; j < KT / 16; ++j) {
+                            // the j-th 16-wide K step starts two core matrices (256 bytes) later
+                            const uint32_t k16 = st4 + 16u * j;
 #pragma unroll
-                            for (int q = 0; q < kTcMaxMma; ++q) {
-                                if (q >= nmma) break;
-                                // the j-th 16-wide K step starts two core matrices (256 bytes) later
-                                const uint64_t ad = desc_hi | (uint64_t)((st4 + a_off[q] + 16 * j) & 0x3FFF);
-                                const uint64_t bd = desc_hi | (uint64_t)((st4 + b_off[q] + 16 * j) & 0x3FFF);
-                                tc::mma_f16(dcol[q], ad, bd, idesc[q], 1u);
-                            }
+                            for (int q = 0; q < kTcMaxMma; ++q)
+                                if (q < nmma)
+                                    tc::mma_f16(pdc[q] + dbuf, desc_a | (uint64_t)(pa[q] + k16),
+                                                desc_b | (uint64_t)(pb[q] + k16), pid[q], 1u);
                         }
                         tc::mma_commit(&empty[s]);
                     }
-                    if (!stop) tc::mma_commit(accum_full);
+                    if (!stop) tc::mma_commit(&accum_full[buf]);
                 }
             }
             // every MMA issued by this thread completes before TMEM is released
@@ -521,22 +566,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
         }
         __syncwarp();
     } else {
-        const int quad = warp & 3, half = (warp - 2) >> 2;
-        const uint32_t tbase = tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(half * EC);
-        tc_zero_release<BN>(p, tbase, tmem_empty, lane);  // the slots start at zero
+        // warp w: TMEM lane quadrant w % 4, column part (w - first) / 4
+        const int quad = warp & 3, part = (warp - kTcEpiWarp0) >> 2;
+        const uint32_t tbase = tmem_base + ((uint32_t)(quad * 32) << 16) + (uint32_t)(part * EC);
+        for (int b = 0; b < p.nbuf; ++b)  // the slots start at zero
+            tc_zero_release<BN, EC>(p, tbase + (uint32_t)b * kTcBufCols, &tmem_empty[b], lane);
         uint32_t unit = 0;
         bool stop = false;
         for (int t = blockIdx.x; t < p.ntiles && !stop; t += gridDim.x) {
             TcUnit u;
             tc_resolve<BN>(p, t, u);
             const int64_t row = (int64_t)u.tm * kTcBM + quad * 32 + lane;
-            const int64_t col0 = (int64_t)u.tn * BN + half * EC;
+            const int64_t col0 = (int64_t)u.tn * BN + part * EC;
             for (int c0 = 0; c0 < u.k_tiles; c0 += p.chunk_tiles, ++unit) {
                 // converged warp, warp-uniform outcome: the TMEM loads below are
                 // warp-collective (lanes past the last row leave the previous
                 // unit's stores early)
                 __syncwarp();
-                const bool waited = tc::mbar_wait(accum_full, unit & 1u);
+                const uint32_t buf = unit % (uint32_t)p.nbuf, use = unit / (uint32_t)p.nbuf;
+                const bool waited = tc::mbar_wait(&accum_full[buf], use & 1u);
                 if (!__all_sync(0xffffffffu, waited && !*abort_flag)) {
                     if (!waited) atomicExch(p.err, kTcErrEpilogueWait);
                     *abort_flag = 1;
@@ -546,10 +594,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
                 tc::tc_fence_after();
                 const int mode = c0 > 0 ? 1 : (u.beta != 0.0 ? 2 : 0);
                 if constexpr (F64)
-                    tc_epilogue_f64<BN, EC>(p, u, tbase, tmem_empty, row, col0, mode, lane,
-                                            colexp_all + (warp - 2) * 64);
+                    tc_epilogue_f64<BN, EC>(p, u, tbase + buf * kTcBufCols, &tmem_empty[buf], row, col0, mode, lane,
+                                            colexp_all + (warp - kTcEpiWarp0) * EC);
                 else
-                    tc_epilogue_f32<BN, EC>(p, u, tbase, tmem_empty, row, col0, mode, lane);
+                    tc_epilogue_f32<BN, EC>(p, u, tbase + buf * kTcBufCols, &tmem_empty[buf], row, col0, mode, lane);
             }
         }
     }
@@ -574,7 +622,7 @@ struct Operand {
 // all tiles and K chunks described by p: single-problem mode (p.tiles null,
 // k_tiles_total K tiles) or grouped mode (p.tiles / p.problems set,
 // `ntiles_grouped` tiles). k_chunk_tiles: K tiles per TMEM accumulation.
-// p.a_stack / b_stack / a_groups / b_groups describe the operand stacks.
+// p.a_stack / b_stack / a_groups / b_blocks describe the operand stacks.
 int launch_tc_gemm(rstsr_ctx* ctx, int kt, TcGemmParams p, int k_tiles_total, int k_chunk_tiles,
                    int64_t ntiles_grouped = 0);
 
