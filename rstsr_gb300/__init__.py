@@ -17,6 +17,9 @@ from .tensor import (  # noqa: F401
     argreduce_axes,
     asarray,
     assign,
+    autotune_gemm,
+    autotune_load,
+    autotune_save,
     binary,
     binary_inplace,
     binary_scalar,

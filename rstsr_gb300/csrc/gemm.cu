@@ -587,10 +587,4 @@ int rstsr_cuda_gemm_grouped(rstsr_ctx* ctx, rstsr_dtype t, const rstsr_gemm_prob
 
 int32_t rstsr_cuda_last_ozaki_slices(void) { return last_ozaki_slices(); }
 
-int rstsr_cuda_autotune_gemm(rstsr_ctx*, rstsr_dtype, int64_t, int64_t, int64_t, const rstsr_gemm_opts*, int32_t*) {
-    return fail(RSTSR_ERR_UNIMPLEMENTED, "autotune not built");
-}
-int rstsr_cuda_autotune_save(const char*) { return fail(RSTSR_ERR_UNIMPLEMENTED, "autotune not built"); }
-int rstsr_cuda_autotune_load(const char*) { return fail(RSTSR_ERR_UNIMPLEMENTED, "autotune not built"); }
-
 }  // extern "C"

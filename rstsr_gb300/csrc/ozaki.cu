@@ -392,7 +392,12 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     g_last_slices = f64 ? L : 0;
     const int S = L;
     constexpr int BN = kTcBN;
-    const int kt = kt_for_stages(S, BN);
+    // kernel configuration: the autotuned one for this shape class, if any
+    int64_t maxm = 0, maxn = 0;
+    for (const auto& q : probs) maxm = std::max(maxm, q.M), maxn = std::max(maxn, q.N);
+    const TuneConfig tune = tune_config(mode, S, maxm, maxn, maxk);
+    int kt = kt_for_stages(S, BN);
+    if (tune.kt && (kTcSmemMax - 1024 - kTcSmemTail) / ((size_t)S * (kTcBM + BN) * tune.kt * 2) >= 2) kt = tune.kt;
     const int lkt = kt == 64 ? 6 : kt == 32 ? 5 : 4;
     const int pitch = (maxk + kt - 1) / kt * kt;
     // slice stacks in the tile layouts; the row groups / blocks past the last
@@ -446,6 +451,7 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     p.row_exp = exps;
     p.col_exp = exps ? (b_items.empty() ? exps : exps + rows_a) : nullptr;
     p.err = ctx->dev_err;
+    p.group_m = tune.group;
     // FP32 accumulation truncates: Ozaki chunks of <= 1024 keep levels 0 to 3
     // exact; the f32 split sums chunks of 512 in C
     const int chunk = f64 ? std::max(1, 1024 / kt) : 512 / kt;

@@ -45,4 +45,13 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
                    const std::vector<SplitItem>& b_items, const std::vector<SplitProblem>& probs, int slices,
                    bool symmetric);
 
+// Tensor-core kernel configuration chosen by the autotuner (autotune.cu):
+// K tile width (16, 32 or 64; 0 = the default rule) and raster group height
+// (row tiles per group / symmetric band; 0 = the kernel default). The code
+// kt | group << 8 is what rstsr_cuda_autotune_gemm reports.
+struct TuneConfig {
+    int kt, group;
+};
+TuneConfig tune_config(SplitMode mode, int slices, int64_t M, int64_t N, int64_t K);
+
 }  // namespace rstsr

@@ -56,11 +56,12 @@ int launch_tc_gemm(rstsr_ctx* ctx, int kt, TcGemmParams p, int k_tiles_total, in
     } else {
         p.tiles_m = (p.M + kTcBM - 1) / kTcBM;
         p.tiles_n = (p.N + BN - 1) / BN;
-        if (p.group_m <= 0) p.group_m = 8;
+        const int group = p.group_m;  // 0: defaults (8 row tiles a group, bands of 16)
+        p.group_m = group > 0 ? group : 8;
         if (p.symmetric) {
             if (p.M != p.N) return fail(RSTSR_ERR_INVALID_LAYOUT, "symmetric product must be square");
             // bands of at least 16 row tiles (2048 rows), at most kTcMaxBands of them
-            p.band_rows = std::max(16, (p.tiles_m + kTcMaxBands - 1) / kTcMaxBands);
+            p.band_rows = std::max(group > 0 ? group : 16, (p.tiles_m + kTcMaxBands - 1) / kTcMaxBands);
             p.nbands = (p.tiles_m + p.band_rows - 1) / p.band_rows;
             ntiles = 0;
             for (int g = 0; g < p.nbands; ++g) {

@@ -769,3 +769,26 @@ def matmul_into(c: Tensor, a: Tensor, b: Tensor, alpha: float = 1.0, beta: float
         a.device.default_order, C.byref(opts),
     )
     return c
+
+
+def autotune_gemm(device: DeviceCuda, dtype, m: int, n: int, k: int, precision: int = 0, slices: int = 0) -> int:
+    """Time the split-GEMM kernel configurations on an m x n x k problem of
+    `dtype` (f64 Ozaki / f32 bf16 split) and keep the fastest for that shape
+    class; returns its code kt | group << 8."""
+    opts = _lib.GemmOpts()
+    opts.precision = precision
+    opts.ozaki_slices = slices
+    best = C.c_int32(0)
+    call("rstsr_cuda_autotune_gemm", device.ctx, dtype_code(dtype), C.c_int64(m), C.c_int64(n), C.c_int64(k),
+         C.byref(opts), C.byref(best))
+    return int(best.value)
+
+
+def autotune_save(path: str) -> None:
+    """Write the autotune table as text."""
+    call("rstsr_cuda_autotune_save", str(path).encode())
+
+
+def autotune_load(path: str) -> None:
+    """Replace the autotune table by the one in `path`."""
+    call("rstsr_cuda_autotune_load", str(path).encode())

@@ -274,3 +274,22 @@ def test_graph_captured_chain_matches_eager(dev):
     np.testing.assert_array_equal(out.to_numpy(), eager)
     want = (a @ b + bias).sum(axis=1)
     assert rel_err(eager, want) <= F64_TOL
+
+
+@pytest.mark.parametrize("dtype,tol,slices", [(np.float64, F64_TOL, 7), (np.float32, F32_TOL, 0)])
+def test_autotune_picks_config_and_results_stay_correct(dev, tmp_path, dtype, tol, slices):
+    code = rt.autotune_gemm(dev, dtype, 512, 512, 512, slices=slices)
+    kt, group = code & 0xFF, code >> 8
+    assert kt in (16, 32, 64) and group in (4, 8, 16, 32)
+    # a problem of the same shape class (log2 extents rounded up: 9, 9, 9) runs with that config
+    rng = np.random.default_rng(11)
+    a = rng.uniform(-1, 1, (500, 480)).astype(dtype)
+    b = rng.uniform(-1, 1, (480, 300)).astype(dtype)
+    c = rt.matmul(rt.asarray(a, dev), rt.asarray(b, dev), slices=slices).to_numpy()
+    assert rel_err(c, ref64(a, b)) <= tol
+    path = tmp_path / "tuned.txt"
+    rt.autotune_save(path)
+    mode = "ozaki" if dtype == np.float64 else "bf16x3"
+    nsl = "7" if dtype == np.float64 else "3"
+    assert [mode, nsl, "9", "9", "9", str(kt), str(group)] in [l.split() for l in path.read_text().splitlines()]
+    rt.autotune_load(path)  # round trip through the file
