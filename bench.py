@@ -443,11 +443,26 @@ def run_gemm_section(dev, stream):
     sec_ref = _time_events(stream, lambda: tb.T @ tb, 1)
     got = torch.as_tensor(c.to_numpy()).cuda()
     err = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
+    # tensor work of the split kernel: L(L+1)/2 bf16 slice products on every
+    # computed 128x64 tile (lower triangle of the symmetric product), K padded
+    # to 16; against the measured cuBLAS bf16 peak (the whole call is timed, so
+    # the statistics and split kernels count against it)
+    tiles_m, tiles_n = -(-Q // 128), -(-Q // 64)
+    ntiles = sum(tiles_m - j // 2 for j in range(min(2 * tiles_m, tiles_n)))
+    bf16_flops = 2.0 * ntiles * 128 * 64 * (-(-P // 16) * 16) * slices * (slices + 1) // 2
+    try:
+        peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"])
+        peak_src = "measured (MEASURED_PEAKS.json bf16_tflops)"
+    except Exception:
+        peak, peak_src = 1900.0, "fallback"
     out["c3_ozaki_f64"] = {
         "shape": "Bm^T Bm, m=n=15000, k=1000 (SYRK path)", "tflops": round(flops / sec / 1e12, 2),
         "ms": round(sec * 1e3, 3), "slices": slices, "rel_err_frobenius": err,
         "native_fp64_cublas_tflops": round(flops / sec_ref / 1e12, 3), "native_ms": round(sec_ref * 1e3, 2),
         "speedup_vs_native_fp64": round(sec_ref / sec, 1), "flop_count": "2mnk (full product)",
+        "roofline": {"bound": "tensor", "achieved": round(bf16_flops / sec / 1e12, 1), "peak": peak,
+                     "unit": "TFLOP/s", "frac": round(bf16_flops / sec / 1e12 / peak, 3),
+                     "peak_source": peak_src, "work": "bf16 slice products of the computed tiles"},
     }
     del c, ref, got, tb
     torch.cuda.empty_cache()
@@ -473,6 +488,33 @@ def run_gemm_section(dev, stream):
         del a, b, ta, tb2, c, fa, fb, ref, sref, got
         torch.cuda.empty_cache()
     return out
+
+
+def run_c3_only(args):
+    """Only the Ozaki contraction C = Bm^T Bm with Bm [1000, cols] (cols =
+    15000 is the full workload; smaller for profiling), timed over --steps
+    calls after --warmup; one JSON line."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    dev = rt.DeviceCuda(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev.set_stream(stream.cuda_stream)
+    rng = np.random.default_rng(0)
+    P, Q = 1000, args.c3_cols
+    bm = rng.standard_normal((P, Q)) * np.exp(-0.01 * np.arange(P))[:, None]
+    t = rt.asarray(bm, dev)
+    c = rt.empty((Q, Q), np.float64, dev)
+    for _ in range(max(args.warmup - 1, 0)):
+        rt.matmul_into(c, t.t(), t, 1.0, 0.0)
+    sec = _time_events(stream, lambda: rt.matmul_into(c, t.t(), t, 1.0, 0.0), max(args.steps, 1))
+    flops = 2.0 * Q * Q * P
+    return {"metric": "f64 Ozaki-split GEMM TFLOP/s", "value": round(flops / sec / 1e12, 2), "unit": "TFLOP/s",
+            "ms_per_step": round(sec * 1e3, 3), "steps": args.steps, "warmup": args.warmup,
+            "slices": int(rt.lib().rstsr_cuda_last_ozaki_slices()),
+            "config": {"workload": f"Bm^T Bm, Bm [1000, {Q}] (SYRK path)"}}
 
 
 def run_batched_section(dev, stream):
@@ -775,8 +817,12 @@ def main():
     # restrict the workload (profiling a small case): comma-separated subsets
     ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
+    ap.add_argument("--only", default="", choices=["", "c3"], help="c3: only the Ozaki contraction")
+    ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.only == "c3":
+        res = run_c3_only(args)
+    elif args.impl == "reference":
         res = run_reference(args)
     else:
         res = run_gpu(args)
