@@ -656,36 +656,54 @@ def run_e2e(wl, dev, stream, args, world):
         )
         pinned.append((ha, hb, hc, outs))
 
+    # three streams: inputs in, compute, results out; case i+1 uploads while
+    # case i computes and earlier results download (the C2C link is full duplex).
+    # The context's stream is switched per phase (rstsr_cuda_ctx_set_stream);
+    # events order the phases of one case.
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    s_comp = stream
+    n = len(wl.cases)
+    ev_in = [torch.cuda.Event() for _ in range(n)]
+    ev_comp = [torch.cuda.Event() for _ in range(n)]
+
     def step():
         h2d = d2h = 0
-        for c, (ha, hb, hc, outs) in zip(wl.cases, pinned):
+        for i, (c, (ha, hb, hc, outs)) in enumerate(zip(wl.cases, pinned)):
+            dev.set_stream(s_in.cuda_stream)
             for host, t in ((ha, c["a"]), (hb, c["b"]), (hc, c["c"])):
                 nb = host.numel() * host.element_size()
                 rc = lib.rstsr_cuda_memcpy_h2d(dev.ctx, C.c_void_p(t.ptr), C.c_void_p(host.data_ptr()), C.c_size_t(nb))
                 assert rc == 0
                 h2d += nb
+            ev_in[i].record(s_in)
+            s_comp.wait_event(ev_in[i])
+            dev.set_stream(s_comp.cuda_stream)
             for op in ("to_contig", "fma", "sum", "argmax"):
                 wl.run_op(c, op)
+            ev_comp[i].record(s_comp)
+            s_out.wait_event(ev_comp[i])
+            dev.set_stream(s_out.cuda_stream)
             for key, t in (("perm", c["out_perm"] if c["copy"] else None), ("d", c["d"]), ("s", c["sum_out"]),
                            ("g", c["arg_out"])):
                 if t is None:
                     continue
                 nb = outs[key].numel()
-                # asynchronous device->host copy on the context stream
+                # asynchronous device->host copy (pinned destination)
                 rc = lib.rstsr_cuda_memcpy_d2d(dev.ctx, C.c_void_p(outs[key].data_ptr()), C.c_void_p(t.ptr),
                                                C.c_size_t(nb))
                 assert rc == 0
                 d2h += nb
+        dev.set_stream(s_comp.cuda_stream)
         return h2d, d2h
 
     for _ in range(max(1, args.warmup // 2)):
         step()
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
     steps = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
     for _ in range(steps):
         h2d, d2h = step()
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()  # a step ends when its last result is on the host
     t = (time.perf_counter() - t0) / steps
     if world > 1:
         tt = torch.tensor([t], device="cuda")
