@@ -36,6 +36,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+from rstsr_gb300 import replicas  # noqa: E402
+
 SHAPE = (32, 64, 128, 128)
 CSHAPE = (1, 64, 1, 128)
 N = int(np.prod(SHAPE))
@@ -261,8 +263,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
         torch.cuda.synchronize()
 
     for _ in range(args.warmup):
@@ -283,13 +284,10 @@ def run_gpu(args):
     if clocks:
         clocks.__exit__()
     launches = dev.launch_count() - l0
-    t_ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(t.item())
     step_bytes = wl.total_bytes()
-    value = step_bytes * world / (t_ms * 1e-3) / 1e9
+    rate, t_s = replicas.whole_job_rate(step_bytes, ev0.elapsed_time(ev1) / args.steps * 1e-3, "cuda")
+    t_ms = t_s * 1e3
+    value = rate / 1e9
 
     # per-operation timing (dominant kernel for the roofline), same stream
     per_op = {}
@@ -704,12 +702,8 @@ def run_e2e(wl, dev, stream, args, world):
     for _ in range(steps):
         h2d, d2h = step()
         torch.cuda.synchronize()  # a step ends when its last result is on the host
-    t = (time.perf_counter() - t0) / steps
-    if world > 1:
-        tt = torch.tensor([t], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
-    return {"value": round(wl.total_bytes() * world / t / 1e9, 1), "unit": "GB/s",
+    rate, t = replicas.whole_job_rate(wl.total_bytes(), (time.perf_counter() - t0) / steps, "cuda")
+    return {"value": round(rate / 1e9, 1), "unit": "GB/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 3)}
 
 
