@@ -241,10 +241,23 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         p.vec = vec ? 1 : 0;
     } else {
         // column regime: a warp reads 32 neighbouring outputs' elements per
-        // step (one 128/256-byte segment), so enough CTAs must be resident
-        // to keep ~40 KB per SM in flight: aim for 8 CTAs per SM
+        // step. When kept dim 0 is contiguous in the input (and everything is
+        // aligned), each thread takes OV neighbouring outputs with one
+        // OV-wide vector load per reduced element; measured on GB300 the
+        // scalar form reached 22 % of DRAM bandwidth (f32 sum_axes over an
+        // F-ordered tensor, 4096 outputs), latency-bound with ~20 KB in
+        // flight per SM. Enough CTAs must be resident to keep ~40 KB per SM
+        // in flight: aim for two waves of 4 CTAs per SM.
         p.glog = 0;
-        const int64_t gx = (p.nout + kRedThreads - 1) / kRedThreads;
+        const int OV = es >= 16 ? 1 : (16 / (int)es >= 4 ? 4 : 16 / (int)es);
+        bool cv = OV > 1 && p.k.nd > 0 && p.k.in_stride[0] == 1 && (p.k.shape[0] % OV) == 0;
+        const int64_t vbytes = (int64_t)OV * (int64_t)es;
+        if (cv) cv = ((reinterpret_cast<uintptr_t>(a) + (uintptr_t)(La.offset * (int64_t)es)) % vbytes) == 0;
+        for (int i = 1; cv && i < p.k.nd; ++i) cv = (std::llabs(p.k.in_stride[i]) * (int64_t)es) % vbytes == 0;
+        for (int i = 0; cv && i < p.r.nd; ++i) cv = (std::llabs(p.r.stride[i]) * (int64_t)es) % vbytes == 0;
+        p.ocol = cv ? OV : 1;
+        const int64_t opc = (int64_t)kRedThreads * p.ocol;
+        const int64_t gx = (p.nout + opc - 1) / opc;
         const int64_t col_target = 8 * (int64_t)ctx->num_sms;
         int64_t nsplit = 1;
         if (gx < col_target && p.nred > 16)

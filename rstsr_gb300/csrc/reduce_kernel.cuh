@@ -71,6 +71,7 @@ struct RedParams {
     int32_t vec;     // reduced dim 0 is contiguous and aligned: VEC-wide loads
     int32_t nsplit;  // chunks of the reduced range (gridDim.y)
     int32_t op;      // rstsr_reduce_op (finalisation)
+    int32_t ocol;    // column regime with vector loads: outputs per thread (1 = scalar)
     int64_t chunk;   // reduced elements per chunk
     void* partial;   // [nsplit][nout] accumulators, or null
     const void* in;
@@ -384,8 +385,89 @@ __device__ __forceinline__ int64_t red_offset(const RedSpace& r, uint32_t e, int
     return off;
 }
 
+// Outputs per thread of the vectorised column regime: a 16-byte (f64: two,
+// 4-byte types: four) or smaller load covers that many neighbouring outputs.
+template <typename T>
+constexpr int red_col_vec() {
+    return 16 / sizeof(T) >= 4 ? 4 : (16 / sizeof(T) >= 2 ? 2 : 1);
+}
+
+// Column regime with vector loads (p.ocol = red_col_vec<T>()): the innermost
+// kept dim is contiguous in the input, so OV neighbouring outputs read one
+// OV-wide vector per reduced element; a warp reads 32 * OV * sizeof(T) bytes
+// per step instead of 32 * sizeof(T), with OV accumulators per thread.
+template <typename T, int KIND>
+__device__ __forceinline__ void reduce_colvec(const RedParams& p) {
+    using R = Red<T, KIND>;
+    using Acc = typename R::Acc;
+    constexpr int OV = red_col_vec<T>();
+    const int64_t o0 = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * OV;
+    if (o0 >= p.nout) return;  // nout is a multiple of OV
+    const T* __restrict__ in = reinterpret_cast<const T*>(p.in);
+    int64_t base = p.in_off;
+    {
+        uint32_t e = (uint32_t)o0;
+        for (int i = 0; i < p.k.nd - 1; ++i) {
+            uint32_t q = p.k.div[i].div(e);
+            base += (int64_t)(e - q * p.k.shape[i]) * p.k.in_stride[i];
+            e = q;
+        }
+        if (p.k.nd > 0) base += (int64_t)e * p.k.in_stride[p.k.nd - 1];
+    }
+    Acc acc[OV];
+#pragma unroll
+    for (int j = 0; j < OV; ++j) acc[j] = R::init();
+    const int64_t rb = (int64_t)blockIdx.y * p.chunk;
+    const int64_t re = min(p.nred, rb + p.chunk);
+    for (int64_t r0 = rb; r0 < re; r0 += kRedUnroll) {
+        RVec<T, OV> v[kRedUnroll];
+        int64_t li[kRedUnroll];
+#pragma unroll
+        for (int u = 0; u < kRedUnroll; ++u)
+            if (r0 + u < re) {
+                const int64_t off = red_offset(p.r, (uint32_t)(r0 + u), &li[u]);
+                v[u] = *reinterpret_cast<const RVec<T, OV>*>(in + base + off);
+            }
+#pragma unroll
+        for (int u = 0; u < kRedUnroll; ++u)
+            if (r0 + u < re) {
+#pragma unroll
+                for (int j = 0; j < OV; ++j) R::fold(acc[j], v[u].v[j], li[u]);
+            }
+    }
+    if (p.partial) {
+        Acc* part = reinterpret_cast<Acc*>(p.partial) + (int64_t)blockIdx.y * p.nout + o0;
+#pragma unroll
+        for (int j = 0; j < OV; ++j) part[j] = acc[j];
+        return;
+    }
+    int64_t oo = p.out_off;
+    {
+        uint32_t e = (uint32_t)o0;
+        for (int i = 0; i < p.k.nd - 1; ++i) {
+            uint32_t q = p.k.div[i].div(e);
+            oo += (int64_t)(e - q * p.k.shape[i]) * p.k.out_stride[i];
+            e = q;
+        }
+        if (p.k.nd > 0) oo += (int64_t)e * p.k.out_stride[p.k.nd - 1];
+    }
+    // the OV outputs are neighbours along kept dim 0
+#pragma unroll
+    for (int j = 0; j < OV; ++j)
+        reinterpret_cast<typename R::Out*>(p.out)[oo + j * p.k.out_stride[0]] = R::fin(acc[j], p.op, p.nred);
+}
+
+// Outputs handled by one CTA.
+__host__ __device__ inline int64_t red_outputs_per_cta(const RedParams& p) {
+    return (int64_t)(kRedThreads >> p.glog) * (p.ocol > 1 ? p.ocol : 1);
+}
+
 template <typename T, int KIND>
 __global__ void __launch_bounds__(kRedThreads) reduce_kernel(const RedParams p) {
+    if (p.ocol > 1) {
+        if constexpr (red_col_vec<T>() > 1) reduce_colvec<T, KIND>(p);
+        return;
+    }
     using R = Red<T, KIND>;
     using Acc = typename R::Acc;
     constexpr int VEC = 16 / sizeof(T) > 0 ? 16 / sizeof(T) : 1;
@@ -516,7 +598,7 @@ constexpr size_t acc_size() {
 // `p` must be fully planned except for the scratch pointer.
 template <typename T, int KIND>
 int launch_reduce(rstsr_ctx* ctx, RedParams p) {
-    const int opc = kRedThreads >> p.glog;  // outputs per CTA
+    const int64_t opc = red_outputs_per_cta(p);
     const int64_t gx = (p.nout + opc - 1) / opc;
     if (gx > INT32_MAX || p.nsplit > 65535) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "reduction too large");
     void* scratch = nullptr;

@@ -45,7 +45,7 @@ static int scratch_address(int device, void** out) {
 template <typename T>
 static int launch_sum_noalloc(cudaStream_t stream, RedParams p, void* scratch) {
     using Acc = typename Red<T, kRedSum>::Acc;
-    const int opc = kRedThreads >> p.glog;
+    const int64_t opc = red_outputs_per_cta(p);
     const int64_t gx = (p.nout + opc - 1) / opc;
     if (gx > INT32_MAX || p.nsplit > 65535) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "reduction too large");
     if (p.nsplit > 1) {
