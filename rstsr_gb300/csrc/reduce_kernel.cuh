@@ -263,25 +263,37 @@ struct Red<T, kRedAny> {
 // never accepted, except that a NaN at logical index 0 makes the answer 0 (the
 // serial fold of cpu_serial/reduction.rs:425-477 starts from that element and
 // no comparison against NaN succeeds afterwards).
+//
+// The empty accumulator holds the worst value (-inf / the type's minimum for
+// argmax) at index INT64_MAX, so "strictly better, or equal at a smaller
+// index" covers it without a separate test, and the fold selects without
+// branches (the comparison-and-select chain bounded the argmax kernels).
 template <typename T, bool IS_MAX>
 struct RedArg {
     using Acc = AccArg<T>;
     using Out = uint64_t;
-    __device__ static Acc init() { return {(T)0, INT64_MAX, 0}; }
+    __device__ static T start() {
+        if constexpr (std::is_floating_point<T>::value) {
+            return IS_MAX ? -(T)INFINITY : (T)INFINITY;
+        } else if constexpr (std::is_signed<T>::value) {
+            const T mn = (T)((UnsignedOfR<T>)1 << (sizeof(T) * 8 - 1));
+            return IS_MAX ? mn : (T)~mn;
+        } else {
+            return IS_MAX ? (T)0 : (T)~(T)0;
+        }
+    }
+    __device__ static Acc init() { return {start(), INT64_MAX, 0}; }
     __device__ static bool better(T x, int64_t ix, T v, int64_t iv) {
-        if (iv == INT64_MAX) return true;
-        if (IS_MAX ? (x > v) : (x < v)) return true;
-        return x == v && ix < iv;
+        return (IS_MAX ? (x > v) : (x < v)) | ((x == v) & (ix < iv));
     }
     __device__ static void fold(Acc& s, T x, int64_t lidx) {
         if (is_nan_v(x)) {
             if (lidx == 0) s.nan0 = 1;
             return;
         }
-        if (better(x, lidx, s.v, s.idx)) {
-            s.v = x;
-            s.idx = lidx;
-        }
+        const bool take = better(x, lidx, s.v, s.idx);
+        s.v = take ? x : s.v;
+        s.idx = take ? lidx : s.idx;
     }
     __device__ static void merge(Acc& s, const Acc& o) {
         s.nan0 |= o.nan0;
@@ -305,11 +317,10 @@ template <bool IS_MAX>
 struct RedArgF64 {
     using Acc = AccArg<int64_t>;
     using Out = uint64_t;
-    __device__ static Acc init() { return {0, INT64_MAX, 0}; }
+    // keys of non-NaN doubles lie strictly inside (INT64_MIN, INT64_MAX)
+    __device__ static Acc init() { return {IS_MAX ? INT64_MIN : INT64_MAX, INT64_MAX, 0}; }
     __device__ static bool better(int64_t x, int64_t ix, int64_t v, int64_t iv) {
-        if (iv == INT64_MAX) return true;
-        if (IS_MAX ? (x > v) : (x < v)) return true;
-        return x == v && ix < iv;
+        return (IS_MAX ? (x > v) : (x < v)) | ((x == v) & (ix < iv));
     }
     __device__ static void fold(Acc& s, double xd, int64_t lidx) {
         int64_t b = __double_as_longlong(xd);
@@ -319,10 +330,9 @@ struct RedArgF64 {
         }
         if (b == INT64_MIN) b = 0;  // -0.0 -> +0.0
         const int64_t key = b >= 0 ? b : (b ^ INT64_MAX);
-        if (better(key, lidx, s.v, s.idx)) {
-            s.v = key;
-            s.idx = lidx;
-        }
+        const bool take = better(key, lidx, s.v, s.idx);
+        s.v = take ? key : s.v;
+        s.idx = take ? lidx : s.idx;
     }
     __device__ static void merge(Acc& s, const Acc& o) {
         s.nan0 |= o.nan0;
