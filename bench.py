@@ -415,6 +415,48 @@ def _time_events(stream, fn, reps):
     return e0.elapsed_time(e1) / reps * 1e-3
 
 
+class _CublasEmulated:
+    """cuBLAS GEMM with an emulated compute type, a comparator only: FP64
+    through fixed-point emulation (CUBLAS_COMPUTE_64F_EMULATED_FIXEDPOINT) and
+    FP32 through three bf16 terms (CUBLAS_COMPUTE_32F_EMULATED_16BFX9), with the
+    emulation strategy set to always emulate. Column-major, as cuBLAS is."""
+
+    F64_FIXEDPOINT, F32_BF16X9 = 79, 78
+
+    def __init__(self, stream):
+        lib = None
+        for name in ("libcublas.so.13", "/usr/local/cuda/lib64/libcublas.so.13"):
+            try:
+                lib = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        if lib is None:
+            raise RuntimeError("libcublas.so.13 not found")
+        self.lib = lib
+        self.h = C.c_void_p()
+        if lib.cublasCreate_v2(C.byref(self.h)) != 0:
+            raise RuntimeError("cublasCreate failed")
+        lib.cublasSetStream_v2(self.h, C.c_void_p(stream.cuda_stream))
+        if lib.cublasSetEmulationStrategy(self.h, 2) != 0:  # CUBLAS_EMULATION_STRATEGY_EAGER
+            raise RuntimeError("cublasSetEmulationStrategy failed")
+        lib.cublasGemmEx.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                     C.c_int, C.c_int, C.c_int]
+
+    def gemm(self, ta, tb, m, n, k, a, lda, b, ldb, c, ldc, f64, compute):
+        one = C.c_double(1.0) if f64 else C.c_float(1.0)
+        zero = C.c_double(0.0) if f64 else C.c_float(0.0)
+        dt = 1 if f64 else 0  # CUDA_R_64F / CUDA_R_32F
+        st = self.lib.cublasGemmEx(self.h, ta, tb, m, n, k, C.byref(one), C.c_void_p(a), dt, lda, C.c_void_p(b), dt,
+                                   ldb, C.byref(zero), C.c_void_p(c), dt, ldc, compute, -1)
+        if st != 0:
+            raise RuntimeError(f"cublasGemmEx returned {st}")
+
+    def close(self):
+        self.lib.cublasDestroy_v2(self.h)
+
+
 def run_gemm_section(dev, stream):
     """The GEMM half of the metric: the f64 electronic-structure contraction
     C = Bm^T Bm (Bm = B[P=1000, i=50, a=300] reshaped to 1000 x 15000, entries
@@ -462,6 +504,36 @@ def run_gemm_section(dev, stream):
                      "unit": "TFLOP/s", "frac": round(bf16_flops / sec / 1e12 / peak, 3),
                      "peak_source": peak_src, "work": "bf16 slice products of the computed tiles"},
     }
+    # comparator: cuBLAS's own fixed-point FP64 emulation, C = X X^T with X the
+    # column-major [15000, 1000] view of Bm
+    try:
+        cb = _CublasEmulated(stream)
+        ce = torch.empty((Q, Q), dtype=torch.float64, device="cuda")
+        fn = lambda: cb.gemm(0, 1, Q, Q, P, tb.data_ptr(), Q, tb.data_ptr(), Q, ce.data_ptr(), Q, True,
+                             cb.F64_FIXEDPOINT)
+        sec_e = _time_events(stream, fn, 1)
+        out["c3_ozaki_f64"]["cublas_emulated_fp64_fixedpoint"] = {
+            "tflops": round(flops / sec_e / 1e12, 2), "ms": round(sec_e * 1e3, 3),
+            "rel_err_frobenius": (torch.linalg.norm(ce - ref) / torch.linalg.norm(ref)).item()}
+        del ce
+        cb.close()
+    except Exception as exc:  # the comparator is optional
+        out["c3_ozaki_f64"]["cublas_emulated_fp64_fixedpoint"] = {"unavailable": str(exc)[:200]}
+    # CPU baseline: host BLAS dsyrk (the DeviceOpenBLAS call) on a bounded sample
+    try:
+        from scipy.linalg import blas as sblas
+
+        qs = 3000
+        xs = np.ascontiguousarray(bm[:, :qs])
+        sblas.dsyrk(1.0, xs, trans=1)
+        t0 = time.perf_counter()
+        sblas.dsyrk(1.0, xs, trans=1)
+        tc = time.perf_counter() - t0
+        out["c3_ozaki_f64"]["cpu_baseline"] = {
+            "value": round(2.0 * qs * qs * P / tc / 1e12, 4), "unit": "TFLOP/s", "cores": os.cpu_count(),
+            "kind": "host BLAS dsyrk (scipy)", "sample": f"Bm[:, :{qs}]^T Bm[:, :{qs}], 2mnk flops"}
+    except Exception as exc:
+        out["c3_ozaki_f64"]["cpu_baseline"] = {"unavailable": str(exc)[:200]}
     del c, ref, got, tb
     torch.cuda.empty_cache()
     for name, (m, n, k) in (("c4_split_f32_8192", (8192, 8192, 8192)), ("c4_split_f32_tall", (65536, 256, 256))):
@@ -483,6 +555,19 @@ def run_gemm_section(dev, stream):
             "cublas_sgemm_tflops": round(2.0 * m * n * k / sec_s / 1e12, 2),
             "cublas_sgemm_rel_err_vs_fp64": (torch.linalg.norm(sref - ref) / nr).item(),
         }
+        try:  # comparator: cuBLAS BF16x9 emulation of FP32 (row-major C = A B as col-major C^T = B^T A^T)
+            cb = _CublasEmulated(stream)
+            ce = torch.empty((m, n), dtype=torch.float32, device="cuda")
+            fn = lambda: cb.gemm(0, 0, n, m, k, fb.data_ptr(), n, fa.data_ptr(), k, ce.data_ptr(), n, False,
+                                 cb.F32_BF16X9)
+            sec_e = _time_events(stream, fn, 3)
+            out[name]["cublas_emulated_bf16x9"] = {
+                "tflops": round(2.0 * m * n * k / sec_e / 1e12, 2), "ms": round(sec_e * 1e3, 3),
+                "rel_err_vs_fp64": (torch.linalg.norm(ce.double() - ref) / nr).item()}
+            del ce
+            cb.close()
+        except Exception as exc:
+            out[name]["cublas_emulated_bf16x9"] = {"unavailable": str(exc)[:200]}
         del a, b, ta, tb2, c, fa, fb, ref, sref, got
         torch.cuda.empty_cache()
     return out

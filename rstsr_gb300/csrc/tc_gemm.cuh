@@ -292,11 +292,61 @@ __device__ __forceinline__ void tc_load_slot(uint32_t tbase, int a, uint32_t (&r
     tc::tmem_ld_wait();
 }
 
+// Per-warp staging tile for C: each lane holds one row of the warp's 32 x EC
+// block, so direct stores from registers touch 32 rows per instruction (the
+// L1 then serialises 32 wavefronts). Through the tile, an instruction covers
+// 32 / W rows of W neighbouring columns (W = 8 for 8-byte, 16 for 4-byte
+// elements). Measured on GB300 before: the f32 split's epilogue spent ~25k
+// cycles per K chunk on the read-modify-write of C.
+constexpr int kTcStageBytes = 32 * 9 * 8;  // 32 rows x (8 + 1) doubles or (16 + 1) floats
+
+template <typename T, int EC>
+__device__ __forceinline__ void warp_store_block(T* C, int64_t ldc, int64_t r0, int64_t c0, int64_t M, int64_t N,
+                                                 bool symmetric, const T (&v)[EC], T* stg, int lane) {
+    constexpr int W = sizeof(T) == 8 ? 8 : 16;  // columns per pass
+    constexpr int P = W + 1;                    // padded row pitch
+    constexpr int RPI = 32 / W;                 // rows per instruction
+#pragma unroll
+    for (int h = 0; h < EC / W; ++h) {
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < W; ++i) stg[lane * P + i] = v[h * W + i];
+        __syncwarp();
+#pragma unroll
+        for (int it = 0; it < 32 / RPI; ++it) {
+            const int rr = it * RPI + lane / W, cc = lane % W;
+            const int64_t row = r0 + rr, col = c0 + h * W + cc;
+            if (row < M && col < N && !(symmetric && col > row)) C[row * ldc + col] = stg[rr * P + cc];
+        }
+    }
+}
+
+template <typename T, int EC>
+__device__ __forceinline__ void warp_load_block(const T* C, int64_t ldc, int64_t r0, int64_t c0, int64_t M,
+                                                int64_t N, T (&v)[EC], T* stg, int lane) {
+    constexpr int W = sizeof(T) == 8 ? 8 : 16;
+    constexpr int P = W + 1;
+    constexpr int RPI = 32 / W;
+#pragma unroll
+    for (int h = 0; h < EC / W; ++h) {
+        __syncwarp();
+#pragma unroll
+        for (int it = 0; it < 32 / RPI; ++it) {
+            const int rr = it * RPI + lane / W, cc = lane % W;
+            const int64_t row = r0 + rr, col = c0 + h * W + cc;
+            stg[rr * P + cc] = (row < M && col < N) ? C[row * ldc + col] : (T)0;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < W; ++i) v[h * W + i] = stg[lane * P + i];
+    }
+}
+
 // f64 epilogue of one unit for this thread's row and EC columns from col0.
 template <int BN, int EC>
 __device__ __forceinline__ void tc_epilogue_f64(const TcGemmParams& p, const TcUnit& u, uint32_t tbase,
                                                 uint64_t* tmem_empty, int64_t row, int64_t col0, int mode,
-                                                int lane, int* colexp) {
+                                                int lane, int* colexp, double* stg) {
     long long fx[EC];
     float fs[EC];  // FP32 sum of the slots: non-finite iff a slot is (inf / NaN inputs)
 #pragma unroll
@@ -325,39 +375,38 @@ __device__ __forceinline__ void tc_epilogue_f64(const TcGemmParams& p, const TcU
         colexp[j] = (u.col_exp && col < u.N) ? u.col_exp[col] : 0;
     }
     __syncwarp();
-    if (row >= u.M) return;
-    const int rexp = (u.row_exp ? u.row_exp[row] : 0) + p.exp_bias - 37;
-    const int ncol = (int)(u.N - col0 < (int64_t)EC ? u.N - col0 : (int64_t)EC);
-    // the products as doubles, in place of their fixed-point sums
+    // every lane takes part in the staged loads and stores below; rows past
+    // the last one compute garbage that is never stored
+    const int rexp = (u.row_exp && row < u.M ? u.row_exp[row] : 0) + p.exp_bias - 37;
+    double x[EC];
 #pragma unroll
     for (int i = 0; i < EC; ++i) {
         const int e = rexp + colexp[i];
-        double x;
-        if (!fixed_to_double(fx[i], e, &x) || !isfinite(fs[i]))
-            x = epilogue_rare(fx[i], e, isnan(fs[i]) ? 2 : isinf(fs[i]) ? (fs[i] > 0 ? 1 : -1) : 0);
-        if (u.alpha != 1.0) x *= u.alpha;
-        fx[i] = __double_as_longlong(x);
+        if (!fixed_to_double(fx[i], e, &x[i]) || !isfinite(fs[i]))
+            x[i] = epilogue_rare(fx[i], e, isnan(fs[i]) ? 2 : isinf(fs[i]) ? (fs[i] > 0 ? 1 : -1) : 0);
+        if (u.alpha != 1.0) x[i] *= u.alpha;
     }
-    double* Cd = reinterpret_cast<double*>(u.C) + row * u.ldc;
-    if (mode != 0) {
-        // C of the later K chunks / beta C: all loads first (independent)
-        double c[EC];
+    double* Cd = reinterpret_cast<double*>(u.C);
+    const int64_t r0 = row - lane;
+    if (mode != 0) {  // C of the later K chunks / beta C, 8 columns at a time
 #pragma unroll
-        for (int i = 0; i < EC; ++i) c[i] = i < ncol ? Cd[col0 + i] : 0.0;
+        for (int h = 0; h < EC / 8; ++h) {
+            double c[8];
+            warp_load_block<double, 8>(Cd, u.ldc, r0, col0 + 8 * h, u.M, u.N, c, stg, lane);
 #pragma unroll
-        for (int i = 0; i < EC; ++i) {
-            const double x = __longlong_as_double(fx[i]);
-            fx[i] = __double_as_longlong(mode == 1 ? x + c[i] : fma(u.beta, c[i], x));
+            for (int i = 0; i < 8; ++i)
+                x[8 * h + i] = mode == 1 ? x[8 * h + i] + c[i] : fma(u.beta, c[i], x[8 * h + i]);
         }
     }
+    warp_store_block<double, EC>(Cd, u.ldc, r0, col0, u.M, u.N, u.symmetric != 0, x, stg, lane);
+    if (u.symmetric && row < u.M) {
+        // the mirror of the lower triangle: lanes are neighbouring rows, so
+        // these stores are contiguous along row `col` of C
 #pragma unroll
-    for (int i = 0; i < EC; ++i) {
-        if (i >= ncol) break;
-        const int64_t col = col0 + i;
-        if (u.symmetric && col > row) continue;  // upper triangle: written by the mirror
-        const double x = __longlong_as_double(fx[i]);
-        Cd[col0 + i] = x;
-        if (u.symmetric && col != row) reinterpret_cast<double*>(u.C)[col * u.ldc + row] = x;
+        for (int i = 0; i < EC; ++i) {
+            const int64_t col = col0 + i;
+            if (col < u.N && col < row) Cd[col * u.ldc + row] = x[i];
+        }
     }
 }
 
@@ -366,7 +415,7 @@ __device__ __forceinline__ void tc_epilogue_f64(const TcGemmParams& p, const TcU
 template <int BN, int EC>
 __device__ __forceinline__ void tc_epilogue_f32(const TcGemmParams& p, const TcUnit& u, uint32_t tbase,
                                                 uint64_t* tmem_empty, int64_t row, int64_t col0, int mode,
-                                                int lane) {
+                                                int lane, float* stg) {
     float s0[EC], t[EC];
     for (int a = 0; a < p.nslots; ++a) {
         uint32_t r[EC];
@@ -379,21 +428,14 @@ __device__ __forceinline__ void tc_epilogue_f32(const TcGemmParams& p, const TcU
         }
     }
     tc_zero_release<BN, EC>(p, tbase, tmem_empty, lane);
-    if (row >= u.M) return;
     const float af = (float)u.alpha, bf = (float)u.beta;
-    float* Cf = reinterpret_cast<float*>(u.C) + row * u.ldc;
-    const int ncol = (int)(u.N - col0 < (int64_t)EC ? u.N - col0 : (int64_t)EC);
-    // C of the later K chunks / beta C: all loads first (independent), then compute and store
+    float* Cf = reinterpret_cast<float*>(u.C);
+    const int64_t r0 = row - lane;
     float c[EC];
-    if (mode != 0) {
-#pragma unroll
-        for (int i = 0; i < EC; ++i) c[i] = i < ncol ? Cf[col0 + i] : 0.f;
-    }
+    if (mode != 0) warp_load_block<float, EC>(Cf, u.ldc, r0, col0, u.M, u.N, c, stg, lane);
+    float y[EC];
 #pragma unroll
     for (int i = 0; i < EC; ++i) {
-        if (i >= ncol) break;
-        const int64_t col = col0 + i;
-        if (u.symmetric && col > row) continue;
         const float ph = af * s0[i], pl = fmaf(af, s0[i], -ph);
         float ch = 0.f, cl = 0.f;
         if (mode == 1) {
@@ -404,16 +446,23 @@ __device__ __forceinline__ void tc_epilogue_f32(const TcGemmParams& p, const TcU
         }
         const float sh = ph + ch, bb = sh - ph;
         const float se = (ph - (sh - bb)) + (ch - bb);
-        const float y = sh + (se + pl + cl + af * t[i]);
-        Cf[col0 + i] = y;
-        if (u.symmetric && col != row) reinterpret_cast<float*>(u.C)[col * u.ldc + row] = y;
+        y[i] = sh + (se + pl + cl + af * t[i]);
+    }
+    warp_store_block<float, EC>(Cf, u.ldc, r0, col0, u.M, u.N, u.symmetric != 0, y, stg, lane);
+    if (u.symmetric && row < u.M) {
+#pragma unroll
+        for (int i = 0; i < EC; ++i) {
+            const int64_t col = col0 + i;
+            if (col < u.N && col < row) Cf[col * u.ldc + row] = y[i];
+        }
     }
 }
 
 // Dynamic shared memory: the stages, then kTcSmemTail bytes of barriers,
-// TMEM slot, abort flag (256 bytes) and the epilogue warps' column-exponent
-// slots (kTcEpiCols ints each), plus 1024 bytes of alignment slack in front.
-constexpr size_t kTcSmemTail = 256 + kTcEpiWarps * kTcEpiCols * 4;
+// TMEM slot, abort flag (256 bytes), the epilogue warps' column-exponent
+// slots (kTcEpiCols ints each) and their C staging tiles (kTcStageBytes
+// each), plus 1024 bytes of alignment slack in front.
+constexpr size_t kTcSmemTail = 256 + kTcEpiWarps * kTcEpiCols * 4 + kTcEpiWarps * kTcStageBytes;
 constexpr size_t kTcSmemMax = 232448;
 
 template <int KT, int BN, bool F64>
@@ -430,6 +479,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* colexp_all = reinterpret_cast<int*>(reinterpret_cast<uint8_t*>(full) + 256);
+    uint8_t* stage_all = reinterpret_cast<uint8_t*>(colexp_all + kTcEpiWarps * kTcEpiCols);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t stages = (uint32_t)p.stages;
@@ -593,11 +643,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
                 }
                 tc::tc_fence_after();
                 const int mode = c0 > 0 ? 1 : (u.beta != 0.0 ? 2 : 0);
+                uint8_t* stg = stage_all + (size_t)(warp - kTcEpiWarp0) * kTcStageBytes;
                 if constexpr (F64)
                     tc_epilogue_f64<BN, EC>(p, u, tbase + buf * kTcBufCols, &tmem_empty[buf], row, col0, mode, lane,
-                                            colexp_all + (warp - kTcEpiWarp0) * EC);
+                                            colexp_all + (warp - kTcEpiWarp0) * EC,
+                                            reinterpret_cast<double*>(stg));
                 else
-                    tc_epilogue_f32<BN, EC>(p, u, tbase + buf * kTcBufCols, &tmem_empty[buf], row, col0, mode, lane);
+                    tc_epilogue_f32<BN, EC>(p, u, tbase + buf * kTcBufCols, &tmem_empty[buf], row, col0, mode, lane,
+                                            reinterpret_cast<float*>(stg));
             }
         }
     }

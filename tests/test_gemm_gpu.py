@@ -293,3 +293,19 @@ def test_autotune_picks_config_and_results_stay_correct(dev, tmp_path, dtype, to
     nsl = "7" if dtype == np.float64 else "3"
     assert [mode, nsl, "9", "9", "9", str(kt), str(group)] in [l.split() for l in path.read_text().splitlines()]
     rt.autotune_load(path)  # round trip through the file
+
+
+def test_ozaki_against_exact_dot_products(dev):
+    """Sampled entries of the C3-shaped SYRK against exact rational sums."""
+    from fractions import Fraction
+
+    rng = np.random.default_rng(0)
+    P, Q = 1000, 512
+    bm = rng.standard_normal((P, Q)) * np.exp(-0.01 * np.arange(P))[:, None]
+    t = rt.asarray(bm, dev)
+    c = rt.matmul(t.t(), t).to_numpy()
+    pairs = [tuple(int(v) for v in rng.integers(0, Q, 2)) for _ in range(24)]
+    cols = {j: [Fraction(float(x)) for x in bm[:, j]] for pair in pairs for j in pair}
+    exact = np.array([float(sum(a * b for a, b in zip(cols[i], cols[j]))) for i, j in pairs])
+    got = np.array([c[i, j] for i, j in pairs])
+    assert np.linalg.norm(got - exact) / np.linalg.norm(exact) <= F64_TOL
