@@ -58,16 +58,36 @@ __device__ __forceinline__ SplitItem seg_at(const SegArg& a, int i) { return a.n
 // ------------------------------------------------------------- statistics
 
 // The A items and the B items of one call are handled by the same launches:
-// blockIdx.z < a.n selects an A item, the rest select B items, whose rows
-// follow the A rows (rows_a of them) in the statistics arrays.
+// items are numbered A first, then B; B rows follow the A rows (rows_a of
+// them) in the statistics arrays. The grid is flat: item i owns blocks
+// [blk0, blk0 + ceil(R / 32) * kblk) of 32 rows x 32 columns, so a grouped
+// call of many small items launches only the blocks that have work (a grid
+// sized for the largest item over every item left most blocks idle: 1 ms of
+// a 512-problem call on GB300).
 struct SegPair {
     SegArg a, b;
     int32_t rows_a;
 };
 
-__device__ __forceinline__ SplitItem pair_item(const SegPair& sp, int z, bool& is_b) {
-    is_b = z >= sp.a.n;
-    return is_b ? seg_at(sp.b, z - sp.a.n) : seg_at(sp.a, z);
+__device__ __forceinline__ int pair_blk0(const SegPair& sp, int i) {
+    return i < sp.a.n ? (sp.a.n <= 2 ? sp.a.inl[i].blk0 : sp.a.dev[i].blk0)
+                      : (sp.b.n <= 2 ? sp.b.inl[i - sp.a.n].blk0 : sp.b.dev[i - sp.a.n].blk0);
+}
+
+// The item of flat block `b` and the block's first row and column in it.
+__device__ __forceinline__ SplitItem pair_block(const SegPair& sp, int64_t b, bool& is_b, int& r0, int& k0) {
+    int lo = 0, hi = sp.a.n + sp.b.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pair_blk0(sp, mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    is_b = lo >= sp.a.n;
+    const SplitItem it = is_b ? seg_at(sp.b, lo - sp.a.n) : seg_at(sp.a, lo);
+    const int64_t local = b - it.blk0;
+    r0 = (int)(local / it.kblk) * 32;
+    k0 = (int)(local % it.kblk) * 32;
+    return it;
 }
 
 // GB300 executes FP64 arithmetic at a small fraction of its integer and FP32
@@ -88,8 +108,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) row_stats_kernel(const SegPair segs, unsigned long long* __restrict__ maxbits,
                                                         double* __restrict__ sumabs) {
     bool is_b;
-    const SplitItem it = pair_item(segs, blockIdx.z, is_b);
-    const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+    int r0, k0;
+    const SplitItem it = pair_block(segs, blockIdx.x, is_b, r0, k0);
     if (r0 >= it.R || k0 >= it.K) return;  // uniform per block
     const int base = (is_b ? segs.rows_a : 0) + it.row0;
     __shared__ unsigned long long smax[8][33];
@@ -149,6 +169,25 @@ __global__ void __launch_bounds__(256) row_stats_kernel(const SegPair segs, unsi
     }
 }
 
+// The exponent spread of each side: max over rows of log2(row max / row mean
+// |x|) for the A rows (out[0]) and the B rows (out[1]), as the bits of
+// non-negative floats (ordered like the values). Grid: row blocks x items.
+__global__ void __launch_bounds__(256) spread_kernel(const SegPair segs, const unsigned long long* __restrict__ maxbits,
+                                                     const double* __restrict__ sumabs, unsigned int* __restrict__ out) {
+    const int z = blockIdx.y;
+    const bool is_b = z >= segs.a.n;
+    const SplitItem it = is_b ? seg_at(segs.b, z - segs.a.n) : seg_at(segs.a, z);
+    const int r = blockIdx.x * 256 + threadIdx.x;
+    if (r >= it.R) return;
+    const int row = (is_b ? segs.rows_a : 0) + it.row0 + r;
+    const double mx = __longlong_as_double((long long)maxbits[row]);
+    const double mean = sumabs[row] / (double)(it.K > 1 ? it.K : 1);
+    if (mx > 0 && mean > 0) {
+        const float sp = (float)log2(mx / mean);
+        if (sp > 0.f) atomicMax(&out[is_b ? 1 : 0], __float_as_uint(sp));
+    }
+}
+
 // ------------------------------------------------------------------ split
 
 // Ozaki slices of one double x of a row with exponent e_r: y = x 2^-e_r as the
@@ -198,8 +237,8 @@ __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitc
                                                     int32_t* __restrict__ exps, __nv_bfloat16* __restrict__ out_a,
                                                     __nv_bfloat16* __restrict__ out_b) {
     bool is_b;
-    const SplitItem it = pair_item(segs, blockIdx.z, is_b);
-    const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
+    int r0, k0;
+    const SplitItem it = pair_block(segs, blockIdx.x, is_b, r0, k0);
     if (r0 >= it.R || k0 >= pitch) return;  // uniform per block
     const int base = (is_b ? segs.rows_a : 0) + it.row0;  // statistics row of r = 0
     __shared__ T tile[32][33];
@@ -311,17 +350,28 @@ static int make_segs(rstsr_ctx* ctx, const std::vector<SplitItem>& items, SegArg
     return s;
 }
 
-static dim3 grid_for(const std::vector<SplitItem>& a, const std::vector<SplitItem>& b, int width) {
-    int maxr = 1;
-    for (const auto& it : a) maxr = std::max(maxr, it.R);
-    for (const auto& it : b) maxr = std::max(maxr, it.R);
-    return dim3((unsigned)((width + 31) / 32), (unsigned)((maxr + 31) / 32), (unsigned)(a.size() + b.size()));
+// Number the flat-grid blocks of the items (A items first): 32 x 32 blocks
+// over each item's rows and its K rounded up to 64 (the widest K tile, so
+// the split also zero-fills the K padding any tile width reads). Returns the
+// total block count.
+static int64_t number_blocks(std::vector<SplitItem>& a, std::vector<SplitItem>& b) {
+    int64_t n = 0;
+    for (auto* v : {&a, &b})
+        for (auto& it : *v) {
+            it.blk0 = (int32_t)n;
+            it.kblk = std::max(1, (it.K + 63) / 64 * 2);
+            n += (int64_t)((it.R + 31) / 32) * it.kblk;
+        }
+    return n;
 }
 
-int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>& a_items,
-                   const std::vector<SplitItem>& b_items, const std::vector<SplitProblem>& probs, int slices,
+int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>& a_items_in,
+                   const std::vector<SplitItem>& b_items_in, const std::vector<SplitProblem>& probs, int slices,
                    bool symmetric) {
     if (probs.empty()) return RSTSR_OK;
+    std::vector<SplitItem> a_items = a_items_in, b_items = b_items_in;
+    const int64_t nblocks = number_blocks(a_items, b_items);
+    if (nblocks > INT32_MAX) return fail(RSTSR_ERR_UNIMPLEMENTED, "operands too large for the split GEMM");
     const bool f64 = mode == SplitMode::Ozaki;
     int rows_a = 0, rows_b = 0, maxk = 0;
     for (const auto& it : a_items) rows_a = std::max(rows_a, it.row0 + it.R), maxk = std::max(maxk, it.K);
@@ -355,7 +405,7 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
         auto* sumabs = (double*)(maxbits + nst);
         exps = (int32_t*)(sumabs + nst);
         RSTSR_CUDA_TRY(cudaMemsetAsync(stats, 0, nst * 16, ctx->stream));
-        row_stats_kernel<double><<<grid_for(a_items, b_items, maxk), 256, 0, ctx->stream>>>(segs, maxbits, sumabs);
+        row_stats_kernel<double><<<(unsigned)nblocks, 256, 0, ctx->stream>>>(segs, maxbits, sumabs);
         if ((s = after_launch(ctx, "row_stats_kernel"))) return cleanup(), s;
         L = slices;
         bool capturing = false;
@@ -363,27 +413,26 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
         if (cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess) capturing = cs != cudaStreamCaptureStatusNone;
         if (L <= 0 && capturing) L = 7;  // no host round trip inside a graph capture
         if (L <= 0) {
-            // choose the slice count from the exponent spread (one synchronisation)
-            std::vector<unsigned long long> hm(nst);
-            std::vector<double> hs(nst);
-            cudaMemcpyAsync(hm.data(), maxbits, nst * 8, cudaMemcpyDeviceToHost, ctx->stream);
-            cudaMemcpyAsync(hs.data(), sumabs, nst * 8, cudaMemcpyDeviceToHost, ctx->stream);
+            // choose the slice count from the exponent spread of each side,
+            // reduced on the device: one synchronisation, 8 bytes back
+            void* dsp = nullptr;
+            if ((s = scratch_alloc(ctx, 8, &dsp))) return cleanup(), s;
+            owned.push_back(dsp);
+            RSTSR_CUDA_TRY(cudaMemsetAsync(dsp, 0, 8, ctx->stream));
+            int maxr = 1;
+            for (const auto* v : {&a_items, &b_items})
+                for (const auto& it : *v) maxr = std::max(maxr, it.R);
+            spread_kernel<<<dim3((unsigned)((maxr + 255) / 256), (unsigned)(a_items.size() + b_items.size())), 256, 0,
+                            ctx->stream>>>(segs, maxbits, sumabs, (unsigned int*)dsp);
+            if ((s = after_launch(ctx, "spread_kernel"))) return cleanup(), s;
+            unsigned int hsp[2] = {0, 0};
+            RSTSR_CUDA_TRY(cudaMemcpyAsync(hsp, dsp, 8, cudaMemcpyDeviceToHost, ctx->stream));
             cudaError_t e = cudaStreamSynchronize(ctx->stream);
             if (e != cudaSuccess) return cleanup(), cuda_fail(e, "split GEMM statistics");
-            auto spread = [&](const std::vector<SplitItem>& items, int base) {
-                double sp = 0;
-                for (const auto& it : items)
-                    for (int i = 0; i < it.R; ++i) {
-                        double mx;
-                        memcpy(&mx, &hm[base + it.row0 + i], 8);
-                        const double mean = hs[base + it.row0 + i] / (double)std::max(it.K, 1);
-                        if (mx > 0 && mean > 0) sp = std::max(sp, std::log2(mx / mean));
-                    }
-                return sp;
-            };
-            const double sA = spread(a_items, 0);
-            const double sB = b_items.empty() ? sA : spread(b_items, rows_a);
-            L = auto_levels(sA, sB);
+            float fa, fb;
+            memcpy(&fa, &hsp[0], 4);
+            memcpy(&fb, &hsp[1], 4);
+            L = auto_levels(fa, b_items.empty() ? fa : fb);
         }
         L = std::min(std::max(L, 1), 8);
     } else {
@@ -413,7 +462,7 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     auto* as = (__nv_bfloat16*)sl;
     auto* bs = as + stack_a;
     {
-        const dim3 g = grid_for(a_items, b_items, pitch);
+        const unsigned g = (unsigned)nblocks;
         if (f64)
             split_kernel<double, 0><<<g, 256, 0, ctx->stream>>>(segs, pitch, S, lkt, groups_a, blocks_b, dual ? 1 : 0,
                                                                 maxbits, exps, as, bs);

@@ -18,6 +18,9 @@ struct SplitItem {
     int64_t s_row, s_k;
     int32_t R, K;
     int32_t row0;
+    // set by split_gemm_run: this item's first block in the statistics and
+    // split grids and its blocks along K (32 columns each, K rounded up to 64)
+    int32_t blk0, kblk;
 };
 
 // C[M,N] (row-major, ldc) = alpha * A[ia] * B[ib]^T + beta * C, where A item
