@@ -60,7 +60,7 @@ __device__ __forceinline__ SplitItem seg_at(const SegArg& a, int i) { return a.n
 // The A items and the B items of one call are handled by the same launches:
 // items are numbered A first, then B; B rows follow the A rows (rows_a of
 // them) in the statistics arrays. The grid is flat: item i owns blocks
-// [blk0, blk0 + ceil(R / 32) * kblk) of 32 rows x 32 columns, so a grouped
+// [blk0, blk0 + ceil(R / 32) * kblk) of 32 rows x 64 columns, so a grouped
 // call of many small items launches only the blocks that have work (a grid
 // sized for the largest item over every item left most blocks idle: 1 ms of
 // a 512-problem call on GB300).
@@ -86,7 +86,7 @@ __device__ __forceinline__ SplitItem pair_block(const SegPair& sp, int64_t b, bo
     const SplitItem it = is_b ? seg_at(sp.b, lo - sp.a.n) : seg_at(sp.a, lo);
     const int64_t local = b - it.blk0;
     r0 = (int)(local / it.kblk) * 32;
-    k0 = (int)(local % it.kblk) * 32;
+    k0 = (int)(local % it.kblk) * 64;
     return it;
 }
 
@@ -103,7 +103,25 @@ __device__ __forceinline__ int exp_above(unsigned long long b) {
     return -1010 - __clzll((long long)b);  // subnormal: highest set bit p, m < 2^(p - 1073)
 }
 
-// Per-row max |x| (as |x| bits) and sum |x|.
+// Load the block's 32 x 64 tile of an item into shared memory (zeros outside
+// the item), coalesced along whichever of rows / K is contiguous in memory.
+template <typename T>
+__device__ __forceinline__ void load_tile(const SplitItem& it, int r0, int k0, T (*tile)[65]) {
+    const T* X = (const T*)it.ptr;
+    const int t = threadIdx.x;
+    const bool kfast = it.s_k == 1 || (it.s_row != 1 && llabs(it.s_k) <= llabs(it.s_row));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int rr = kfast ? (t >> 6) + 4 * j : (t & 31);
+        const int kk = kfast ? (t & 63) : (t >> 5) + 8 * j;
+        const int r = r0 + rr, k = k0 + kk;
+        tile[rr][kk] = (r < it.R && k < it.K) ? X[(int64_t)r * it.s_row + (int64_t)k * it.s_k] : (T)0;
+    }
+}
+
+// Per-row max |x| (as |x| bits) and sum |x|: thread t takes row t / 8 of the
+// tile and its 8 consecutive columns, the 8 threads of a row combine by
+// shuffles, one atomic pair per row and block.
 template <typename T>
 __global__ void __launch_bounds__(256) row_stats_kernel(const SegPair segs, unsigned long long* __restrict__ maxbits,
                                                         double* __restrict__ sumabs) {
@@ -111,61 +129,30 @@ __global__ void __launch_bounds__(256) row_stats_kernel(const SegPair segs, unsi
     int r0, k0;
     const SplitItem it = pair_block(segs, blockIdx.x, is_b, r0, k0);
     if (r0 >= it.R || k0 >= it.K) return;  // uniform per block
-    const int base = (is_b ? segs.rows_a : 0) + it.row0;
-    __shared__ unsigned long long smax[8][33];
-    __shared__ double ssum[8][33];
-    const T* X = (const T*)it.ptr;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const bool kfast = it.s_k == 1 || (it.s_row != 1 && llabs(it.s_k) <= llabs(it.s_row));
-    unsigned long long m[4] = {0, 0, 0, 0};
-    double s[4] = {0, 0, 0, 0};
+    __shared__ T tile[32][65];
+    load_tile<T>(it, r0, k0, tile);
+    __syncthreads();
+    const int rr = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
+    unsigned long long mm = 0;
+    double ss = 0.0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int rr = kfast ? ty + 8 * j : tx;
-        const int kk = kfast ? tx : ty + 8 * j;
-        const int r = r0 + rr, k = k0 + kk;
-        if (r < it.R && k < it.K) {
-            const unsigned long long b =
-                (unsigned long long)__double_as_longlong((double)X[(int64_t)r * it.s_row + (int64_t)k * it.s_k]) &
-                0x7FFFFFFFFFFFFFFFull;
-            m[j] = b;
-            s[j] = __longlong_as_double((long long)b);
-        }
+    for (int v = 0; v < 8; ++v) {
+        const unsigned long long b =
+            (unsigned long long)__double_as_longlong((double)tile[rr][kq + v]) & 0x7FFFFFFFFFFFFFFFull;
+        mm = b > mm ? b : mm;
+        ss += __longlong_as_double((long long)b);
     }
-    if (kfast) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            unsigned long long mm = m[j];
-            double ss = s[j];
-            for (int d = 16; d > 0; d >>= 1) {
-                const unsigned long long o = __shfl_down_sync(0xffffffffu, mm, d);
-                mm = o > mm ? o : mm;
-                ss += __shfl_down_sync(0xffffffffu, ss, d);
-            }
-            const int r = r0 + ty + 8 * j;
-            if (tx == 0 && r < it.R) {
-                atomicMax(&maxbits[base + r], mm);
-                atomicAdd(&sumabs[base + r], ss);
-            }
-        }
-    } else {
-        unsigned long long mm = m[0];
-        for (int j = 1; j < 4; ++j) mm = m[j] > mm ? m[j] : mm;
-        double ss = s[0] + s[1] + s[2] + s[3];
-        smax[ty][tx] = mm;
-        ssum[ty][tx] = ss;
-        __syncthreads();
-        if (ty == 0) {
-            for (int i = 1; i < 8; ++i) {
-                mm = smax[i][tx] > mm ? smax[i][tx] : mm;
-                ss += ssum[i][tx];
-            }
-            const int r = r0 + tx;
-            if (r < it.R) {
-                atomicMax(&maxbits[base + r], mm);
-                atomicAdd(&sumabs[base + r], ss);
-            }
-        }
+    for (int d = 4; d > 0; d >>= 1) {
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, mm, d, 8);
+        mm = o > mm ? o : mm;
+        ss += __shfl_down_sync(0xffffffffu, ss, d, 8);
+    }
+    const int r = r0 + rr;
+    if ((threadIdx.x & 7) == 0 && r < it.R) {
+        const int row = (is_b ? segs.rows_a : 0) + it.row0 + r;
+        atomicMax(&maxbits[row], mm);
+        atomicAdd(&sumabs[row], ss);
     }
 }
 
@@ -190,46 +177,27 @@ __global__ void __launch_bounds__(256) spread_kernel(const SegPair segs, const u
 
 // ------------------------------------------------------------------ split
 
-// Ozaki slices of one double x of a row with exponent e_r: y = x 2^-e_r as the
-// fixed-point integer Y = y 2^63 (|Y| < 2^63; bits below 2^-63 of the row
-// maximum are dropped), then balanced base-128 digits from the top,
-// d_s = round(Y / 2^(56 - 7s)) with Y reduced by each digit, so that
-// |d_0| <= 128 and |d_s| <= 64 after it. Slice s is d_s 2^(-7s), exact in
-// bf16. Non-finite x puts itself in slice 0 and zeros after it.
-constexpr int kMaxSlices = 8;
-
-__device__ __forceinline__ void ozaki_digits(double x, int e_r, int S, __nv_bfloat16 (&v)[kMaxSlices]) {
-    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
-    const int E = (int)((u >> 52) & 0x7FF);
-    if (E == 0x7FF) {
-        const uint32_t nan = (u & 0xFFFFFFFFFFFFFull) ? 0x7FC00000u : 0x7F800000u;
-        v[0] = __float2bfloat16_rn(__uint_as_float((uint32_t)(u >> 32) & 0x80000000u | nan));
-#pragma unroll
-        for (int s = 1; s < kMaxSlices; ++s) v[s] = __float2bfloat16_rn(0.f);
-        return;
-    }
-    const long long mant = (long long)(E ? (u & 0xFFFFFFFFFFFFFull) | (1ull << 52) : (u & 0xFFFFFFFFFFFFFull));
-    const int sh = (E ? E : 1) - 1012 - e_r;  // |x| = mant 2^((E ? E : 1) - 1075) < 2^e_r, so Y < 2^63
-    long long Y = sh >= 0 ? mant << sh : (sh > -63 ? mant >> -sh : 0);
-    if (u >> 63) Y = -Y;
-#pragma unroll
-    for (int s = 0; s < kMaxSlices; ++s) {
-        if (s >= S) break;
-        const int k = 56 - 7 * s;
-        const long long d = (Y >> k) + ((Y >> (k - 1)) & 1);  // round half up, no overflow
-        Y -= d << k;
-        v[s] = __float2bfloat16_rn(__int2float_rn((int)d) * __int_as_float((127 - 7 * s) << 23));
-    }
-}
-
 // Cut every item into slices, written into the stack of its side in the
 // tensor-core tile layouts (KT = 2^lkt): A items as tc_offset_a (groups_a row
 // groups, slice stride 8 KT), B items as tc_offset_b (blocks_b 64-row blocks,
 // slice stride 64 KT); with `dual` (a symmetric product, B = A) the A items
 // are written in both layouts. Zero in [K, pitch).
-// MODE 0: Ozaki integer slices (ozaki_digits); the k-tile-0 blocks also store
-//         the row exponents e_r (max_r < 2^e_r) from the row maxima.
+// Thread t takes row t / 8 of the block's 32 x 64 tile and 8 consecutive
+// columns, i.e. one core-matrix row per slice: each slice is one 16-byte
+// store.
+// MODE 0: Ozaki slices of each double x of a row with exponent e_r: y = x 2^-e_r
+//         as the fixed-point integer Y = y 2^63 (|Y| < 2^63; bits below 2^-63
+//         of the row maximum are dropped), then balanced base-128 digits from
+//         the top, d_s = round(Y / 2^(56 - 7s)) with Y reduced by each digit,
+//         so |d_0| <= 128 and |d_s| <= 64 after it. Slice s is d_s 2^(-7s),
+//         exact in bf16; a non-finite x puts itself in slice 0 and zeros after
+//         it. The column-0 threads also store the row exponents e_r.
 // MODE 1: f32 three-term split hi / mid / lo.
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
+           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(hi)) << 16);
+}
+
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitch, int S, int lkt, int groups_a,
                                                     int blocks_b, int dual,
@@ -240,58 +208,93 @@ __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitc
     int r0, k0;
     const SplitItem it = pair_block(segs, blockIdx.x, is_b, r0, k0);
     if (r0 >= it.R || k0 >= pitch) return;  // uniform per block
-    const int base = (is_b ? segs.rows_a : 0) + it.row0;  // statistics row of r = 0
-    __shared__ T tile[32][33];
-    const T* X = (const T*)it.ptr;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const bool kfast = it.s_k == 1 || (it.s_row != 1 && llabs(it.s_k) <= llabs(it.s_row));
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int rr = kfast ? ty + 8 * j : tx;
-        const int kk = kfast ? tx : ty + 8 * j;
-        const int r = r0 + rr, k = k0 + kk;
-        T v = (T)0;
-        if (r < it.R && k < it.K) v = X[(int64_t)r * it.s_row + (int64_t)k * it.s_k];
-        tile[rr][kk] = v;
-    }
+    __shared__ T tile[32][65];
+    load_tile<T>(it, r0, k0, tile);
     __syncthreads();
+    const int rr = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
+    const int r = r0 + rr, kb = k0 + kq;
+    if (r >= it.R || kb >= pitch) return;  // pitch is a multiple of 16: whole runs
+    const int row = it.row0 + r;
     const int KT = 1 << lkt;
+    const size_t kt = (size_t)(kb >> lkt);
+    const size_t inner = (size_t)((((kb & (KT - 1)) >> 3) << 6) + ((row & 7) << 3));
+    uint4* oa = is_b ? nullptr
+                     : reinterpret_cast<uint4*>(out_a + (((kt * groups_a + (size_t)(row >> 3)) * S) << (3 + lkt)) + inner);
+    uint4* ob = (is_b || dual)
+                    ? reinterpret_cast<uint4*>(out_b +
+                                               ((((kt * blocks_b + (size_t)(row >> 6)) * S) * 8 +
+                                                 (size_t)((row >> 3) & 7))
+                                                << (3 + lkt)) +
+                                               inner)
+                    : nullptr;
+    // slice strides in 16-byte units: 8 KT elements (A), 64 KT elements (B)
+    const size_t sa = (size_t)1 << (lkt - 0), sb = (size_t)8 << lkt;
+    if constexpr (MODE == 0) {
+        const int e_r = exp_above(maxbits[(is_b ? segs.rows_a : 0) + row]);
+        if (kb == 0) exps[(is_b ? segs.rows_a : 0) + row] = e_r;
+        // the values as fixed-point integers Y = x 2^(63 - e_r)
+        long long Y[8];
+        uint32_t special = 0;    // bit v: value v is inf / NaN
+        float spv[8];            // its bf16-exact float (slice 0)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int rr = ty + 8 * j;
-        const int r = r0 + rr, k = k0 + tx;
-        if (r >= it.R || k >= pitch) continue;
-        __nv_bfloat16 v[kMaxSlices];
-        if (k >= it.K) {
-#pragma unroll
-            for (int s = 0; s < kMaxSlices; ++s) v[s] = __float2bfloat16_rn(0.f);
-        } else if constexpr (MODE == 0) {
-            const int e_r = exp_above(maxbits[base + r]);
-            if (k == 0) exps[base + r] = e_r;
-            ozaki_digits((double)tile[rr][tx], e_r, S, v);
-        } else {
-            const float x = (float)tile[rr][tx];
-            v[0] = __float2bfloat16_rn(x);
-            const float r1 = x - __bfloat162float(v[0]);
-            v[1] = __float2bfloat16_rn(r1);
-            v[2] = __float2bfloat16_rn(r1 - __bfloat162float(v[1]));
+        for (int v = 0; v < 8; ++v) {
+            const unsigned long long u = (unsigned long long)__double_as_longlong((double)tile[rr][kq + v]);
+            const int E = (int)((u >> 52) & 0x7FF);
+            const long long mant =
+                (long long)(E ? (u & 0xFFFFFFFFFFFFFull) | (1ull << 52) : (u & 0xFFFFFFFFFFFFFull));
+            const int sh = (E ? E : 1) - 1012 - e_r;
+            long long y = sh >= 0 ? mant << (sh < 63 ? sh : 63) : (sh > -63 ? mant >> -sh : 0);
+            if (u >> 63) y = -y;
+            Y[v] = y;
+            spv[v] = 0.f;
+            if (E == 0x7FF) {
+                special |= 1u << v;
+                Y[v] = 0;
+                const uint32_t nan = (u & 0xFFFFFFFFFFFFFull) ? 0x7FC00000u : 0x7F800000u;
+                spv[v] = __uint_as_float(((uint32_t)(u >> 32) & 0x80000000u) | nan);
+            }
         }
-        const int row = it.row0 + r;
-        const size_t kt = (size_t)(k >> lkt);
-        const size_t inner = (size_t)((((k & (KT - 1)) >> 3) << 6) + ((row & 7) << 3) + (k & 7));
-        if (!is_b) {
-            __nv_bfloat16* o = out_a + (((kt * groups_a + (size_t)(row >> 3)) * S) << (3 + lkt)) + inner;
+        for (int sl = 0; sl < S; ++sl) {
+            const int k = 56 - 7 * sl;
+            const float scale = __int_as_float((127 - 7 * sl) << 23);
+            float d[8];
 #pragma unroll
-            for (int s = 0; s < kMaxSlices; ++s)
-                if (s < S) o[(size_t)s << (3 + lkt)] = v[s];
+            for (int v = 0; v < 8; ++v) {
+                const long long dd = (Y[v] >> k) + ((Y[v] >> (k - 1)) & 1);  // round half up
+                Y[v] -= dd << k;
+                d[v] = __int2float_rn((int)dd) * scale;
+                if (sl == 0 && (special >> v) & 1u) d[v] = spv[v];
+            }
+            const uint4 w = make_uint4(pack_bf16(d[0], d[1]), pack_bf16(d[2], d[3]), pack_bf16(d[4], d[5]),
+                                       pack_bf16(d[6], d[7]));
+            if (oa) oa[sl * sa] = w;
+            if (ob) ob[sl * sb] = w;
         }
-        if (is_b || dual) {
-            __nv_bfloat16* o =
-                out_b + ((((kt * blocks_b + (size_t)(row >> 6)) * S) * 8 + (size_t)((row >> 3) & 7)) << (3 + lkt)) +
-                inner;
+    } else {
+        float h[8], m[8], l[8];
 #pragma unroll
-            for (int s = 0; s < kMaxSlices; ++s)
-                if (s < S) o[(size_t)s << (6 + lkt)] = v[s];
+        for (int v = 0; v < 8; ++v) {
+            const float x = (float)tile[rr][kq + v];
+            h[v] = __bfloat162float(__float2bfloat16_rn(x));
+            const float r1 = x - h[v];
+            m[v] = __bfloat162float(__float2bfloat16_rn(r1));
+            l[v] = r1 - m[v];
+        }
+        const uint4 wh = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]),
+                                    pack_bf16(h[6], h[7]));
+        const uint4 wm = make_uint4(pack_bf16(m[0], m[1]), pack_bf16(m[2], m[3]), pack_bf16(m[4], m[5]),
+                                    pack_bf16(m[6], m[7]));
+        const uint4 wl = make_uint4(pack_bf16(l[0], l[1]), pack_bf16(l[2], l[3]), pack_bf16(l[4], l[5]),
+                                    pack_bf16(l[6], l[7]));
+        if (oa) {
+            oa[0] = wh;
+            if (S > 1) oa[sa] = wm;
+            if (S > 2) oa[2 * sa] = wl;
+        }
+        if (ob) {
+            ob[0] = wh;
+            if (S > 1) ob[sb] = wm;
+            if (S > 2) ob[2 * sb] = wl;
         }
     }
 }
@@ -350,7 +353,7 @@ static int make_segs(rstsr_ctx* ctx, const std::vector<SplitItem>& items, SegArg
     return s;
 }
 
-// Number the flat-grid blocks of the items (A items first): 32 x 32 blocks
+// Number the flat-grid blocks of the items (A items first): 32 x 64 blocks
 // over each item's rows and its K rounded up to 64 (the widest K tile, so
 // the split also zero-fills the K padding any tile width reads). Returns the
 // total block count.
@@ -359,7 +362,7 @@ static int64_t number_blocks(std::vector<SplitItem>& a, std::vector<SplitItem>& 
     for (auto* v : {&a, &b})
         for (auto& it : *v) {
             it.blk0 = (int32_t)n;
-            it.kblk = std::max(1, (it.K + 63) / 64 * 2);
+            it.kblk = std::max(1, (it.K + 63) / 64);
             n += (int64_t)((it.R + 31) / 32) * it.kblk;
         }
     return n;
