@@ -393,6 +393,7 @@ def run_gpu(args):
             result["gemm"] = run_gemm_section(dev, stream)
             result["gemm"].update(run_batched_section(dev, stream))
             result["small_f64"] = run_small_section(dev, stream)
+            result["tri_index"] = run_tri_index_section(dev, stream)
         if not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline(args)
     if world > 1:
@@ -720,6 +721,99 @@ def run_small_section(dev, stream):
     return res
 
 
+def run_tri_index_section(dev, stream, n=2048, batch=32, rows=16384, cols=8192):
+    """Packed-triangle and index-selection kernels on resident f64 data:
+    pack_tri 'L' of [batch, n, n] (read the triangle, write the packed
+    vector: 2 * batch * n(n+1)/2 * 8 bytes), unpack_tri 'L' Sy of the packed
+    [batch, n(n+1)/2] (read it once, write both triangles: batch *
+    (n(n+1)/2 + n^2) * 8 bytes), and index_select of half the rows (axis 0)
+    and half the columns (axis 1) of a [rows, cols] matrix, random indices
+    with repeats (read + write of the selected elements). Device time by CUDA
+    events, inputs larger than L2; torch's gather on the same data beside it."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    peak = 6800.0
+    try:
+        peak = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("hbm_gbs", peak)
+    except Exception:
+        pass
+    out = {}
+    rng = np.random.default_rng(0)
+    ntp = n * (n + 1) // 2
+
+    def entry(name, sec, nbytes, launches, torch_sec=None, **kw):
+        gbs = nbytes / sec / 1e9
+        e = {"gbs": round(gbs, 1), "ms": round(sec * 1e3, 4), "bytes": int(nbytes), "frac_hbm": round(gbs / peak, 3),
+             "launches_per_call": int(launches)}
+        if torch_sec:
+            e["torch_gbs"] = round(nbytes / torch_sec / 1e9, 1)
+        e.update(kw)
+        out[name] = e
+
+    m = rng.standard_normal((batch, n, n))
+    tm = rt.asarray(m, dev)
+    del m
+    l0 = dev.launch_count()
+    packed = rt.pack_tri(tm, "L")
+    torch.cuda.synchronize()
+    launches = dev.launch_count() - l0
+    sec = _time_events(stream, lambda: rt.pack_tri(tm, "L"), 5)
+    gm = torch.empty((batch, n, n), dtype=torch.float64, device="cuda")
+    il = torch.tril_indices(n, n, device="cuda")
+    sec_t = _time_events(stream, lambda: gm[:, il[0], il[1]], 3)
+    entry("pack_tril_f64", sec, 2 * batch * ntp * 8, launches, sec_t, shape=[batch, n, n])
+    del gm
+    l0 = dev.launch_count()
+    rt.unpack_tri(packed, "L", "Sy")
+    torch.cuda.synchronize()
+    launches = dev.launch_count() - l0
+    sec = _time_events(stream, lambda: rt.unpack_tri(packed, "L", "Sy"), 5)
+    entry("unpack_tril_sy_f64", sec, batch * (ntp + n * n) * 8, launches, shape=[batch, ntp])
+    del tm, packed, il
+    torch.cuda.empty_cache()
+
+    a = rng.standard_normal((rows, cols))
+    ta = rt.asarray(a, dev)
+    ga = torch.from_numpy(a).cuda()
+    del a
+    ridx = rng.integers(0, rows, rows // 2)
+    l0 = dev.launch_count()
+    rt.index_select(ta, 0, ridx)
+    torch.cuda.synchronize()
+    launches = dev.launch_count() - l0
+    sec = _time_events(stream, lambda: rt.index_select(ta, 0, ridx), 5)
+    gidx = torch.from_numpy(ridx).cuda()
+    sec_t = _time_events(stream, lambda: torch.index_select(ga, 0, gidx), 5)
+    entry("index_select_rows_f64", sec, 2 * (rows // 2) * cols * 8, launches, sec_t, shape=[rows, cols],
+          indices=rows // 2)
+    cidx = rng.integers(0, cols, cols // 2)
+    sec = _time_events(stream, lambda: rt.index_select(ta, 1, cidx), 5)
+    gidx = torch.from_numpy(cidx).cuda()
+    sec_t = _time_events(stream, lambda: torch.index_select(ga, 1, gidx), 5)
+    entry("index_select_cols_f64", sec, 2 * rows * (cols // 2) * 8, launches, sec_t, shape=[rows, cols],
+          indices=cols // 2)
+    del ta, ga
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_tri_index_only(args):
+    """Only the packed-triangle / index-selection section (profiling)."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    dev = rt.DeviceCuda(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev.set_stream(stream.cuda_stream)
+    res = run_tri_index_section(dev, stream, n=args.tri_n, batch=args.tri_batch, rows=args.sel_rows,
+                                cols=args.sel_cols)
+    return {"section": "tri_index", "results": res}
+
+
 def run_e2e(wl, dev, stream, args, world):
     """Same step with host buffers: every input copied in (pinned host memory)
     and every result copied out inside the timed region, through the C ABI."""
@@ -914,11 +1008,18 @@ def main():
     # restrict the workload (profiling a small case): comma-separated subsets
     ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
-    ap.add_argument("--only", default="", choices=["", "c3"], help="c3: only the Ozaki contraction")
+    ap.add_argument("--only", default="", choices=["", "c3", "tri_index"],
+                    help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
+    ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
+    ap.add_argument("--tri-batch", type=int, default=32, help="matrices for --only tri_index")
+    ap.add_argument("--sel-rows", type=int, default=16384, help="rows of the index_select source")
+    ap.add_argument("--sel-cols", type=int, default=8192, help="columns of the index_select source")
     args = ap.parse_args()
     if args.only == "c3":
         res = run_c3_only(args)
+    elif args.only == "tri_index":
+        res = run_tri_index_only(args)
     elif args.impl == "reference":
         res = run_reference(args)
     else:

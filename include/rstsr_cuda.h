@@ -48,7 +48,9 @@ typedef enum {
     RSTSR_ERR_DEVICE = 5,            /* RSTSRError::DeviceError (CUDA error) */
     RSTSR_ERR_RUNTIME = 6,           /* RSTSRError::RuntimeError */
     RSTSR_ERR_UNIMPLEMENTED = 7,     /* RSTSRError::UnImplemented */
-    RSTSR_ERR_TIMEOUT = 8            /* a bounded device-side wait gave up */
+    RSTSR_ERR_TIMEOUT = 8,           /* a bounded device-side wait gave up */
+    RSTSR_ERR_INDEX = 9,             /* RSTSRError::IndexError */
+    RSTSR_ERR_AXIS = 10              /* RSTSRError::AxisError */
 } rstsr_status;
 
 /* Element types (the `T` of DeviceRawAPI<T>). U64 is Rust `usize`. */
@@ -324,6 +326,46 @@ int rstsr_cuda_argreduce_axes_into(rstsr_ctx* ctx, int32_t is_max, rstsr_dtype t
 #define RSTSR_NOALLOC_SCRATCH_BYTES (1u << 20)
 int rstsr_cuda_sum_axes_noalloc(void* cuda_stream, rstsr_dtype ta, const void* a, const rstsr_layout* la,
                                 const int64_t* axes, int32_t naxes, void* out, const rstsr_layout* lout);
+
+/* ---------------------------------------------- triangles and indexing */
+
+/* FlagSymm (rstsr-common/src/flags.rs:220-240). For the real element types
+ * of this library He behaves as Sy and Ah as Ay. */
+typedef enum {
+    RSTSR_SYMM_SY = 0,  /* symmetric: mirror = value */
+    RSTSR_SYMM_HE = 1,  /* Hermitian: mirror = conj(value) */
+    RSTSR_SYMM_AY = 2,  /* anti-symmetric: mirror = -value, diagonal 0 */
+    RSTSR_SYMM_AH = 3,  /* anti-Hermitian: mirror = -conj(value), diagonal 0 */
+    RSTSR_SYMM_N = 4    /* no symmetry: only the packed triangle is written */
+} rstsr_symm;
+
+/* OpPackTriAPI::pack_tri (rstsr-core/src/operators/ops/op_tri.rs:3-15; CPU
+ * impl rstsr-native-impl/src/cpu_serial/op_tri.rs:73-144): a (.., n(n+1)/2)
+ * receives the uplo ('L' | 'U') triangle of b (.., n, n), rows packed in
+ * order (for RowMajor; ColMajor reverses all axes and flips uplo first,
+ * feature_rayon/auto_impl/op_tri.rs:7-30). Any dtype. */
+int rstsr_cuda_pack_tri(rstsr_ctx* ctx, rstsr_dtype t, void* a, const rstsr_layout* la,
+                        const void* b, const rstsr_layout* lb, char uplo, rstsr_order order);
+
+/* OpUnpackTriAPI::unpack_tri (op_tri.rs:17-30; cpu_serial/op_tri.rs:148-410):
+ * a (.., n, n) from the packed triangle b (.., n(n+1)/2) and its mirror by
+ * symm. With RSTSR_SYMM_N the other triangle of a is left as it was (the
+ * reference leaves it uninitialised). Float dtypes (F64, F32, F16, BF16), as
+ * the reference's `T: ComplexFloat`. */
+int rstsr_cuda_unpack_tri(rstsr_ctx* ctx, rstsr_dtype t, void* a, const rstsr_layout* la,
+                          const void* b, const rstsr_layout* lb, char uplo, rstsr_symm symm,
+                          rstsr_order order);
+
+/* DeviceIndexSelectAPI::index_select (rstsr-core/src/operators/adv_indexing.rs:8-23;
+ * CPU impl rstsr-native-impl/src/cpu_serial/adv_indexing.rs:3-69):
+ * c[.., k, ..] = a[.., indices[k], ..] along `axis`. `indices` is HOST memory
+ * (the reference's &[usize]); each must be below a's extent on the axis
+ * (RSTSR_ERR_INDEX otherwise); lc's extent on the axis is nindices and its
+ * other extents equal la's. Any dtype. At most 512 indices inside a graph
+ * capture (they are baked into the captured launch). */
+int rstsr_cuda_index_select(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc,
+                            const void* a, const rstsr_layout* la, int32_t axis,
+                            const uint64_t* indices, int64_t nindices);
 
 /* ---------------------------------------------------------------- matmul */
 

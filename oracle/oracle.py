@@ -71,8 +71,12 @@ def lib() -> C.CDLL:
         L.oracle_reduce_axes.argtypes = [I, I, P, LP, C.POINTER(C.c_int64), I, P, LP, I]
         L.oracle_argreduce_axes.argtypes = [I, I, P, LP, C.POINTER(C.c_int64), I, C.POINTER(C.c_uint64), LP, I]
         L.oracle_max_threads.argtypes = []
+        L.oracle_pack_tri.argtypes = [P, LP, P, LP, I, I, I]
+        L.oracle_unpack_tri.argtypes = [P, LP, P, LP, I, I, I, I]
+        L.oracle_index_select.argtypes = [P, LP, P, LP, I, C.POINTER(C.c_uint64), C.c_int64, I]
         for f in (L.oracle_assign, L.oracle_assign_arbitrary, L.oracle_binary, L.oracle_fma, L.oracle_reduce_axes,
-                  L.oracle_argreduce_axes, L.oracle_max_threads):
+                  L.oracle_argreduce_axes, L.oracle_max_threads, L.oracle_pack_tri, L.oracle_unpack_tri,
+                  L.oracle_index_select):
             f.restype = C.c_int
         _lib = L
     return _lib
@@ -173,3 +177,26 @@ def argreduce_axes(is_max: bool, a: Strided, axes, out: Strided, nthreads: int =
     _ok(lib().oracle_argreduce_axes(1 if is_max else 0, DT[a.buf.dtype], _p(a.buf), C.byref(a.layout), ax, len(axes),
                                     out.buf.ctypes.data_as(C.POINTER(C.c_uint64)), C.byref(out.layout), nthreads),
         "argreduce_axes")
+
+
+def pack_tri(dst: Strided, src: Strided, lower: bool, order: int = 0) -> None:
+    """dst (.., n(n+1)/2) <- the lower / upper triangle of src (.., n, n)."""
+    _ok(lib().oracle_pack_tri(_p(dst.buf), C.byref(dst.layout), _p(src.buf), C.byref(src.layout), dst.buf.itemsize,
+                              1 if lower else 0, order), "pack_tri")
+
+
+SYMM = {"Sy": 0, "He": 1, "Ay": 2, "Ah": 3, "N": 4}
+
+
+def unpack_tri(dst: Strided, src: Strided, lower: bool, symm: str = "Sy", order: int = 0) -> None:
+    """dst (.., n, n) <- packed triangle src (.., n(n+1)/2) and its mirror."""
+    _ok(lib().oracle_unpack_tri(_p(dst.buf), C.byref(dst.layout), _p(src.buf), C.byref(src.layout), dst.buf.itemsize,
+                                1 if lower else 0, SYMM[symm], order), "unpack_tri")
+
+
+def index_select(dst: Strided, src: Strided, axis: int, indices) -> None:
+    """dst[.., k, ..] = src[.., indices[k], ..] along `axis`."""
+    idx = np.ascontiguousarray(np.asarray(indices, dtype=np.uint64))
+    _ok(lib().oracle_index_select(_p(dst.buf), C.byref(dst.layout), _p(src.buf), C.byref(src.layout), int(axis),
+                                  idx.ctypes.data_as(C.POINTER(C.c_uint64)), C.c_int64(idx.size), dst.buf.itemsize),
+        "index_select")

@@ -15,6 +15,11 @@
  *                     init/f/f_sum/f_out of auto_impl/reduction.rs:7-716
  *   argreduce_axes    rstsr-native-impl/src/cpu_serial/reduction.rs:425-580
  *                     (row-major fold, ties keep the smaller index)
+ *   pack_tri          rstsr-native-impl/src/cpu_serial/op_tri.rs:26-71
+ *                     (inner_pack_tri{l,u}_general, row loop i, column j)
+ *   unpack_tri        rstsr-native-impl/src/cpu_serial/op_tri.rs:217-410
+ *                     (inner_unpack_tri{l,u}_general for Sy/He/Ay/Ah/N)
+ *   index_select      rstsr-native-impl/src/cpu_serial/adv_indexing.rs:3-69
  *
  * Every function takes `nthreads`: 1 runs the serial semantics; more threads
  * run the same per-output / per-row algorithm split across OpenMP threads the
@@ -573,6 +578,144 @@ int oracle_argreduce_axes(int is_max, int dtype, const void* a, const olayout* l
         case T_I64: ARG_CASE(int64_t)
         default: return 2;
     }
+}
+
+/* ------------------------------------------------------ triangles */
+
+/* Row-major view of a (matrix or packed) layout pair: ColMajor reverses the
+ * axes and flips uplo (feature_rayon/auto_impl/op_tri.rs:20-26). */
+static void reverse_layout(olayout* l) {
+    for (int i = 0, j = l->ndim - 1; i < j; ++i, --j) {
+        int64_t t = l->shape[i];
+        l->shape[i] = l->shape[j];
+        l->shape[j] = t;
+        t = l->stride[i];
+        l->stride[i] = l->stride[j];
+        l->stride[j] = t;
+    }
+}
+
+/* Offset of batch element e (C order over the first nb axes). */
+static int64_t batch_offset(const olayout* l, int nb, int64_t e) {
+    int64_t o = l->offset;
+    for (int d = nb - 1; d >= 0; --d) {
+        int64_t i = e % l->shape[d];
+        e /= l->shape[d];
+        o += i * l->stride[d];
+    }
+    return o;
+}
+
+/* a (.., n(n+1)/2) <- triangle of b (.., n, n). */
+int oracle_pack_tri(void* a, const olayout* la0, const void* b, const olayout* lb0, int esize, int lower, int order) {
+    olayout la = *la0, lb = *lb0;
+    if (order == 1) {
+        reverse_layout(&la);
+        reverse_layout(&lb);
+        lower = !lower;
+    }
+    if (lb.ndim < 2 || la.ndim != lb.ndim - 1) return 1;
+    const int nb = la.ndim - 1;
+    const int64_t n = lb.shape[lb.ndim - 1];
+    const int64_t si = lb.stride[lb.ndim - 2], sj = lb.stride[lb.ndim - 1], sp = la.stride[nb];
+    int64_t nbatch = 1;
+    for (int d = 0; d < nb; ++d) nbatch *= la.shape[d];
+    for (int64_t e = 0; e < nbatch; ++e) {
+        const int64_t oa = batch_offset(&la, nb, e), ob = batch_offset(&lb, nb, e);
+        int64_t idx = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t j0 = lower ? 0 : i, j1 = lower ? i + 1 : n;
+            for (int64_t j = j0; j < j1; ++j, ++idx)
+                memcpy((char*)a + (oa + idx * sp) * esize, (const char*)b + (ob + i * si + j * sj) * esize,
+                       (size_t)esize);
+        }
+    }
+    return 0;
+}
+
+/* Negation of a float element of `esize` bytes: arithmetic for f64 / f32,
+ * the sign bit for the 16-bit formats (IEEE negation). */
+static void neg_elem(void* dst, const void* src, int esize) {
+    if (esize == 8) {
+        double x;
+        memcpy(&x, src, 8);
+        x = -x;
+        memcpy(dst, &x, 8);
+    } else if (esize == 4) {
+        float x;
+        memcpy(&x, src, 4);
+        x = -x;
+        memcpy(dst, &x, 4);
+    } else {
+        uint16_t x;
+        memcpy(&x, src, 2);
+        x ^= 0x8000u;
+        memcpy(dst, &x, 2);
+    }
+}
+
+/* a (.., n, n) <- packed triangle b (.., n(n+1)/2) and its mirror.
+ * symm: 0 Sy, 1 He, 2 Ay, 3 Ah, 4 N (real types: He = Sy, Ah = Ay). */
+int oracle_unpack_tri(void* a, const olayout* la0, const void* b, const olayout* lb0, int esize, int lower,
+                      int symm, int order) {
+    olayout la = *la0, lb = *lb0;
+    if (order == 1) {
+        reverse_layout(&la);
+        reverse_layout(&lb);
+        lower = !lower;
+    }
+    if (la.ndim < 2 || lb.ndim != la.ndim - 1) return 1;
+    const int nb = lb.ndim - 1;
+    const int64_t n = la.shape[la.ndim - 1];
+    const int64_t si = la.stride[la.ndim - 2], sj = la.stride[la.ndim - 1], sp = lb.stride[nb];
+    const int anti = symm == 2 || symm == 3, mirror = symm != 4;
+    int64_t nbatch = 1;
+    for (int d = 0; d < nb; ++d) nbatch *= lb.shape[d];
+    for (int64_t e = 0; e < nbatch; ++e) {
+        const int64_t oa = batch_offset(&la, nb, e), ob = batch_offset(&lb, nb, e);
+        int64_t idx = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t j0 = lower ? 0 : i, j1 = lower ? i + 1 : n;
+            for (int64_t j = j0; j < j1; ++j, ++idx) {
+                const char* v = (const char*)b + (ob + idx * sp) * esize;
+                char* aij = (char*)a + (oa + i * si + j * sj) * esize;
+                char* aji = (char*)a + (oa + j * si + i * sj) * esize;
+                if (anti && i == j) {
+                    memset(aij, 0, (size_t)esize);
+                    continue;
+                }
+                memcpy(aij, v, (size_t)esize);
+                if (!mirror) continue;
+                if (anti)
+                    neg_elem(aji, v, esize);
+                else
+                    memcpy(aji, v, (size_t)esize);
+            }
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------ index_select */
+
+/* c[.., k, ..] = a[.., idx[k], ..] along `axis` (every c element, C order). */
+int oracle_index_select(void* c, const olayout* lc, const void* a, const olayout* la, int axis,
+                        const uint64_t* idx, int64_t nidx, int esize) {
+    if (lc->ndim != la->ndim || axis < 0 || axis >= lc->ndim || lc->shape[axis] != nidx) return 1;
+    for (int64_t k = 0; k < nidx; ++k)
+        if (idx[k] >= (uint64_t)la->shape[axis]) return 2;
+    const int64_t n = lsize(lc);
+    for (int64_t e = 0; e < n; ++e) {
+        int64_t r = e, oc = lc->offset, oa = la->offset;
+        for (int d = lc->ndim - 1; d >= 0; --d) {
+            const int64_t i = r % lc->shape[d];
+            r /= lc->shape[d];
+            oc += i * lc->stride[d];
+            oa += (d == axis ? (int64_t)idx[i] : i) * la->stride[d];
+        }
+        memcpy((char*)c + oc * esize, (const char*)a + oa * esize, (size_t)esize);
+    }
+    return 0;
 }
 
 int oracle_max_threads(void) {

@@ -23,18 +23,23 @@ from .tensor import (  # noqa: F401
     binary,
     binary_inplace,
     binary_scalar,
+    bool_select,
     empty,
     fill,
     fma,
     from_host_layout,
     full,
+    index_select,
     matmul,
     matmul_into,
+    pack_tri,
     reduce_all,
     reduce_axes,
     reduce_axes_into,
+    take,
     to_contig,
     unary,
+    unpack_tri,
     zeros,
 )
 

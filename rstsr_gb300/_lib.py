@@ -29,6 +29,8 @@ class RstsrError(RuntimeError):
         6: "RuntimeError",
         7: "UnImplemented",
         8: "Timeout",
+        9: "IndexError",
+        10: "AxisError",
     }
 
     def __init__(self, code: int, msg: str):
@@ -170,6 +172,12 @@ _SIGS = {
     "rstsr_cuda_argreduce_all": ([_P, _I, _I, _P, _L, C.POINTER(C.c_uint64)], C.c_int),
     "rstsr_cuda_argreduce_axes": ([_P, _I, _I, _P, _L, C.POINTER(C.c_int64), _I, C.POINTER(_P), _L], C.c_int),
     "rstsr_cuda_argreduce_axes_into": ([_P, _I, _I, _P, _L, C.POINTER(C.c_int64), _I, _P, _L], C.c_int),
+    "rstsr_cuda_pack_tri": ([_P, _I, _P, _L, _P, _L, C.c_char, _I], C.c_int),
+    "rstsr_cuda_unpack_tri": ([_P, _I, _P, _L, _P, _L, C.c_char, _I, _I], C.c_int),
+    "rstsr_cuda_index_select": (
+        [_P, _I, _P, _L, _P, _L, C.c_int32, C.POINTER(C.c_uint64), C.c_int64],
+        C.c_int,
+    ),
     "rstsr_cuda_gemm": (
         [_P, _I, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_int64, C.c_double, _P, C.c_int64, _P, C.c_int64,
          C.c_double, _P, C.c_int64, _I, C.POINTER(GemmOpts)],

@@ -792,3 +792,126 @@ def autotune_save(path: str) -> None:
 def autotune_load(path: str) -> None:
     """Replace the autotune table by the one in `path`."""
     call("rstsr_cuda_autotune_load", str(path).encode())
+
+
+# ------------------------------------------------- triangles and indexing
+
+SYMM = {"Sy": 0, "He": 1, "Ay": 2, "Ah": 3, "N": 4}
+
+
+def _uplo_byte(uplo) -> bytes:
+    u = {"L": b"L", "l": b"L", "Lower": b"L", "U": b"U", "u": b"U", "Upper": b"U"}.get(uplo)
+    if u is None:
+        raise RstsrError(2, f"uplo must be 'L' or 'U', got {uplo!r}")
+    return u
+
+
+def _symm_code(symm) -> int:
+    if isinstance(symm, int) and symm in SYMM.values():
+        return symm
+    if symm not in SYMM:
+        raise RstsrError(2, f"unknown symmetry flag {symm!r}")
+    return SYMM[symm]
+
+
+def _tri_out_order(t: Tensor) -> int:
+    # pack_tri_f / unpack_tri_f: C if the input prefers C only, F if F only,
+    # else the device's default order (rstsr-core/src/tensor/operators/op_tri.rs:56-63)
+    c, f = t.c_prefer(), t.f_prefer()
+    if c and not f:
+        return ROW_MAJOR
+    if f and not c:
+        return COL_MAJOR
+    return t.device.default_order
+
+
+def pack_tri(t: Tensor, uplo="L") -> Tensor:
+    """pack_tri_f (rstsr-core/src/tensor/operators/op_tri.rs:13-71): the uplo
+    triangle of the trailing (RowMajor) or leading (ColMajor) n x n axes,
+    rows packed in order."""
+    order = t.device.default_order
+    if t.ndim < 2:
+        raise RstsrError(1, "pack_tri needs at least two axes")
+    if order == ROW_MAJOR:
+        n, n2 = t.shape[-2], t.shape[-1]
+        rest = t.shape[:-2]
+    else:
+        n, n2 = t.shape[0], t.shape[1]
+        rest = t.shape[2:]
+    if n != n2:
+        raise RstsrError(1, "the two matrix dimensions should be the same for pack_tri")
+    ntp = n * (n + 1) // 2
+    out_shape = rest + (ntp,) if order == ROW_MAJOR else (ntp,) + rest
+    out = empty(out_shape, t.dtype_code, t.device, order="C" if _tri_out_order(t) == ROW_MAJOR else "F")
+    call("rstsr_cuda_pack_tri", t.device.ctx, t.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
+         C.c_void_p(t.ptr), C.byref(t.layout()), _uplo_byte(uplo), order)
+    return out
+
+
+def unpack_tri(t: Tensor, uplo="L", symm="Sy") -> Tensor:
+    """unpack_tri_f (op_tri.rs:105-162): the n x n matrices whose uplo
+    triangle is packed along the trailing (RowMajor) / leading (ColMajor) axis,
+    the other triangle filled by the symmetry. With symm "N" the other
+    triangle is zero here (the reference leaves it uninitialised)."""
+    order = t.device.default_order
+    if t.ndim < 1:
+        raise RstsrError(1, "unpack_tri needs at least one axis")
+    ntp = t.shape[-1] if order == ROW_MAJOR else t.shape[0]
+    n = int(np.floor(np.sqrt(float(2 * ntp))))
+    if n * (n + 1) // 2 != ntp:
+        raise RstsrError(1, "the packed dimension should be a triangular number for unpack_tri")
+    code = _symm_code(symm)
+    out_shape = t.shape[:-1] + (n, n) if order == ROW_MAJOR else (n, n) + t.shape[1:]
+    out_order = "C" if _tri_out_order(t) == ROW_MAJOR else "F"
+    out = zeros(out_shape, t.dtype_code, t.device, out_order) if code == SYMM["N"] else \
+        empty(out_shape, t.dtype_code, t.device, order=out_order)
+    call("rstsr_cuda_unpack_tri", t.device.ctx, t.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
+         C.c_void_p(t.ptr), C.byref(t.layout()), _uplo_byte(uplo), code, order)
+    return out
+
+
+def index_select(t: Tensor, axis: int, indices) -> Tensor:
+    """index_select_f (rstsr-core/src/tensor/adv_indexing.rs:10-46): gather
+    along `axis`; negative indices count from the end. The output is
+    contiguous in the device's default order."""
+    ndim = t.ndim
+    ax = int(axis)
+    if ax < -ndim or ax >= ndim:
+        raise RstsrError(10, f"axis {axis} out of range for ndim {ndim}")
+    ax %= ndim if ndim else 1
+    nshape = t.shape[ax]
+    idx = np.asarray(list(indices) if not isinstance(indices, np.ndarray) else indices, dtype=np.int64).ravel()
+    idx = np.where(idx < 0, idx + nshape, idx)
+    if idx.size and (idx.min() < 0 or idx.max() >= nshape):
+        raise RstsrError(9, f"invalid index that exceeds shape length at axis {ax}")
+    out_shape = list(t.shape)
+    out_shape[ax] = int(idx.size)
+    out = empty(out_shape, t.dtype_code, t.device, order="C" if t.device.default_order == ROW_MAJOR else "F")
+    host = np.ascontiguousarray(idx.astype(np.uint64))
+    call("rstsr_cuda_index_select", t.device.ctx, t.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
+         C.c_void_p(t.ptr), C.byref(t.layout()), ax, host.ctypes.data_as(C.POINTER(C.c_uint64)),
+         C.c_int64(host.size))
+    return out
+
+
+def take(t: Tensor, indices, axis: int) -> Tensor:
+    """take (adv_indexing.rs:66-78): index_select with the arguments swapped."""
+    return index_select(t, axis, indices)
+
+
+def bool_select(t: Tensor, axis: int, mask) -> Tensor:
+    """bool_select_f (adv_indexing.rs:144-160): index_select of the positions
+    where `mask` is true."""
+    m = np.asarray(mask, dtype=bool).ravel()
+    return index_select(t, axis, np.nonzero(m)[0])
+
+
+Tensor.pack_tri = pack_tri
+Tensor.pack_tril = lambda self: pack_tri(self, "L")
+Tensor.pack_triu = lambda self: pack_tri(self, "U")
+Tensor.unpack_tri = unpack_tri
+Tensor.unpack_tril = lambda self, symm="Sy": unpack_tri(self, "L", symm)
+Tensor.unpack_triu = lambda self, symm="Sy": unpack_tri(self, "U", symm)
+Tensor.index_select = index_select
+Tensor.take = lambda self, indices, axis: take(self, indices, axis)
+Tensor.bool_select = bool_select

@@ -174,10 +174,51 @@ CASES = [
 ]
 
 
+# Triangular packing and index selection (the reference's own unit tests).
+# `fingerprint` is rstsr-core/src/dev_utilities/mod.rs:48-68: the row-major
+# flattening x of the result dotted with cos(0), cos(1), ..., cos(size-1).
+SEL = [1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233]
+TRI_INDEX_CASES = [
+    dict(src="rstsr-core/src/tensor/operators/op_tri.rs:192-208", op="pack_unpack", order="C", uplo="L",
+         buf="arange48", shape=[3, 4, 4], layout="f", packed_slice=[1],
+         expect_packed=[1.0, 4.0, 16.0, 7.0, 19.0, 31.0, 10.0, 22.0, 34.0, 46.0],
+         symm="Sy", unpacked_slice=[0, 1], expect_unpacked=[3.0, 15.0, 18.0, 21.0]),
+    dict(src="rstsr-core/src/tensor/operators/op_tri.rs:210-226", op="pack_unpack", order="F", uplo="U",
+         buf="arange48", shape=[4, 4, 3], layout="c", packed_slice=[None, 1],
+         expect_packed=[1.0, 4.0, 16.0, 7.0, 19.0, 31.0, 10.0, 22.0, 34.0, 46.0],
+         symm="Sy", unpacked_slice=[None, 1, 0], expect_unpacked=[3.0, 15.0, 18.0, 21.0]),
+    dict(src="rstsr-core/src/tensor/operators/op_tri.rs:253-268", op="pack_tril_c_vs_f", order="C",
+         buf="arange16", shape=[4, 4], expect_packed=[0.0, 4.0, 5.0, 8.0, 9.0, 10.0, 12.0, 13.0, 14.0, 15.0]),
+    *[
+        dict(src="rstsr-core/src/tensor/adv_indexing.rs:209-219", op="index_select_fingerprint", order="C",
+             linspace=[1.0, 24.0, 24], shape=[2, 3, 4], axis=ax, indices=[0, 0, 1, -1], expect=e, tol=1e-8)
+        for ax, e in [(0, -31.94175930917264), (1, 3.5719025258942088), (2, -25.648600916145096)]
+    ],
+    *[
+        dict(src="rstsr-core/src/tensor/adv_indexing.rs:220-231", op="index_select_fingerprint", order="F",
+             linspace=[1.0, 24.0, 24], shape=[4, 3, 2], axis=ax, indices=[0, 0, 1, -1], expect=e, tol=1e-8)
+        for ax, e in [(2, -31.94175930917264), (1, 3.5719025258942088), (0, -25.648600916145096)]
+    ],
+    *[
+        dict(src="rstsr-core/src/tensor/adv_indexing.rs:242-254", op="index_select_fingerprint", order="C",
+             linspace=[1.0, 2.0, 256 * 256 * 256], shape=[256, 256, 256], axis=ax, indices=SEL, expect=e, tol=1e-10)
+        for ax, e in [(0, 0.9357016252766746), (1, 1.012193909979973), (2, 1.010735112247236)]
+    ],
+    dict(src="rstsr-core/src/tensor/adv_indexing.rs:233-238", op="index_select", dtype="f64",
+         a=[1.0, 2.0, 3.0, 4.0], axis=0, indices=[], expect=[]),
+    dict(src="rstsr-core/tests/core_func/indexing/test_indexing.rs:96-107", op="index_select", dtype="i32",
+         a=list(range(10)), axis=0, indices=[2, 4, 8], expect=[2, 4, 8]),
+]
+
+
 def main() -> None:
-    out = Path(__file__).resolve().parent / "reference_kats.json"
+    here = Path(__file__).resolve().parent
+    out = here / "reference_kats.json"
     out.write_text(json.dumps(CASES, indent=1) + "\n")
     print(f"wrote {len(CASES)} cases to {out}")
+    out = here / "tri_index_kats.json"
+    out.write_text(json.dumps(TRI_INDEX_CASES, indent=1) + "\n")
+    print(f"wrote {len(TRI_INDEX_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
