@@ -16,7 +16,10 @@
 // kIdxInline indices ride in the kernel parameters (no copy, valid inside a
 // graph capture: the list is baked into the captured launch); longer lists
 // are copied to stream-ordered scratch first.
+#include <atomic>
+
 #include "ew_kernel.cuh"
+#include "tc_ptx.cuh"
 
 namespace rstsr {
 
@@ -25,14 +28,26 @@ namespace {
 constexpr int kIdxInline = 512;
 constexpr int kIsThreads = 256;
 constexpr int kIsUnroll = 4;
+constexpr int64_t kStageMaxBytes = 96 * 1024;  // source row staged in shared memory (two CTAs per SM)
+constexpr int kBulkThreads = 512;
+constexpr int64_t kBulkMinRow = 4096;           // rows staged by bulk copies: 4 KiB ..
+constexpr int64_t kBulkSmem = 200 * 1024;       // .. with 2-4 row buffers in this much shared memory
+constexpr uint32_t kBulkChunk = 32 * 1024;      // bytes per cp.async.bulk
+constexpr int kIsErrStageWait = 5;              // error word: a staged-row wait gave up
 
 struct IsParams {
     DevDims dims;            // inner first
     int axis_dim;            // dims index of the indexed axis, -1 if folded away
     int big;                 // 64-bit index decomposition
     int64_t total;
+    uint32_t nrows;          // product of dims 1.. (row kernel)
     int64_t sc[RSTSR_MAX_NDIM], sa[RSTSR_MAX_NDIM];
     int64_t off_c, off_a;
+    int64_t row_len;         // staged kernel: source elements per row (the axis extent)
+    int stage_vec;           // staged kernel: rows load as 16-byte words
+    int nbuf;                // bulk kernel: row buffers (0: not the bulk kernel)
+    uint32_t buf_stride;     // bulk kernel: bytes between row buffers
+    int* err;                // device error word
     int nidx;                // indices held inline (0: use idx)
     const int64_t* idx;      // device copy of the indices (long lists)
     int64_t inl[kIdxInline];
@@ -84,6 +99,162 @@ __global__ void __launch_bounds__(kIsThreads)
     }
 }
 
+// Innermost dim long (>= one CTA width): a CTA walks whole rows of it, the
+// outer multi-index decomposed once per row; four loads in flight per thread.
+template <typename W>
+__global__ void __launch_bounds__(kIsThreads)
+    index_select_rows_kernel(W* __restrict__ c, const W* __restrict__ a, const __grid_constant__ IsParams p) {
+    __shared__ int64_t sidx[kIdxInline];
+    for (int i = threadIdx.x; i < p.nidx; i += blockDim.x) sidx[i] = p.inl[i];
+    __syncthreads();
+    const int64_t* ix = p.nidx ? sidx : p.idx;
+    const int64_t n0 = p.dims.shape[0], sc0 = p.sc[0], sa0 = p.sa[0];
+    const bool ax0 = p.axis_dim == 0;
+    for (uint32_t row = blockIdx.x; row < p.nrows; row += gridDim.x) {
+        int64_t offc = p.off_c, offa = p.off_a;
+        uint32_t rem = row;
+        for (int d = 1; d < p.dims.ndim; ++d) {
+            const uint32_t q = d + 1 < p.dims.ndim ? p.dims.div[d].div(rem) : 0;
+            const int64_t k = (int64_t)(rem - q * p.dims.shape[d]);
+            rem = q;
+            offc += k * p.sc[d];
+            offa += (d == p.axis_dim ? ix[k] : k) * p.sa[d];
+        }
+        for (int64_t k0 = threadIdx.x; k0 < n0; k0 += kIsThreads * kIsUnroll) {
+            W v[kIsUnroll];
+#pragma unroll
+            for (int u = 0; u < kIsUnroll; ++u) {
+                const int64_t k = k0 + (int64_t)u * kIsThreads;
+                if (k < n0) v[u] = a[offa + (ax0 ? ix[k] : k) * sa0];
+            }
+#pragma unroll
+            for (int u = 0; u < kIsUnroll; ++u) {
+                const int64_t k = k0 + (int64_t)u * kIsThreads;
+                if (k < n0) c[offc + k * sc0] = v[u];
+            }
+        }
+    }
+}
+
+// Indexed axis innermost, contiguous in the source, and the selection dense
+// (at least one index per four source elements): gathering straight from
+// global memory would fetch a 32-byte sector per element in random order, so
+// the CTA first copies the whole source row into shared memory with coalesced
+// (16-byte where aligned) loads, then gathers from there with coalesced
+// stores. Two CTAs per SM overlap one's row load with the other's gather.
+template <typename W>
+__global__ void __launch_bounds__(kIsThreads)
+    index_select_staged_kernel(W* __restrict__ c, const W* __restrict__ a, const __grid_constant__ IsParams p) {
+    extern __shared__ uint4 stage_raw[];
+    __shared__ int64_t sidx[kIdxInline];
+    for (int i = threadIdx.x; i < p.nidx; i += blockDim.x) sidx[i] = p.inl[i];
+    const int64_t* ix = p.nidx ? sidx : p.idx;
+    W* row = reinterpret_cast<W*>(stage_raw);
+    const int64_t n0 = p.dims.shape[0], sc0 = p.sc[0], L = p.row_len;
+    const int64_t nvec = L * (int64_t)sizeof(W) / 16;
+    for (uint32_t r = blockIdx.x; r < p.nrows; r += gridDim.x) {
+        int64_t offc = p.off_c, offa = p.off_a;
+        uint32_t rem = r;
+        for (int d = 1; d < p.dims.ndim; ++d) {
+            const uint32_t q = d + 1 < p.dims.ndim ? p.dims.div[d].div(rem) : 0;
+            const int64_t k = (int64_t)(rem - q * p.dims.shape[d]);
+            rem = q;
+            offc += k * p.sc[d];
+            offa += (d == p.axis_dim ? ix[k] : k) * p.sa[d];
+        }
+        __syncthreads();  // the previous row's gathers are done with the stage
+        if (p.stage_vec) {
+            const uint4* src = reinterpret_cast<const uint4*>(a + offa);
+            for (int64_t q0 = threadIdx.x; q0 < nvec; q0 += kIsThreads * kIsUnroll) {
+                uint4 v[kIsUnroll];
+#pragma unroll
+                for (int u = 0; u < kIsUnroll; ++u)
+                    if (q0 + u * kIsThreads < nvec) v[u] = src[q0 + u * kIsThreads];
+#pragma unroll
+                for (int u = 0; u < kIsUnroll; ++u)
+                    if (q0 + u * kIsThreads < nvec) stage_raw[q0 + u * kIsThreads] = v[u];
+            }
+        } else {
+            for (int64_t q0 = threadIdx.x; q0 < L; q0 += kIsThreads * kIsUnroll) {
+                W v[kIsUnroll];
+#pragma unroll
+                for (int u = 0; u < kIsUnroll; ++u)
+                    if (q0 + u * kIsThreads < L) v[u] = a[offa + q0 + u * kIsThreads];
+#pragma unroll
+                for (int u = 0; u < kIsUnroll; ++u)
+                    if (q0 + u * kIsThreads < L) row[q0 + u * kIsThreads] = v[u];
+            }
+        }
+        __syncthreads();
+        for (int64_t k = threadIdx.x; k < n0; k += kIsThreads) c[offc + k * sc0] = row[ix[k]];
+    }
+}
+
+// The staged gather with the rows moved by the copy engine: one CTA per SM
+// keeps nbuf source rows in flight as cp.async.bulk copies (completion counted
+// on one mbarrier per buffer) and gathers from the oldest while the others
+// fill. Every wait is bounded; a CTA that gives up records kIsErrStageWait,
+// waits (bounded) for its copies still in flight, and returns.
+template <typename W>
+__global__ void __launch_bounds__(kBulkThreads)
+    index_select_bulk_kernel(W* __restrict__ c, const W* __restrict__ a, const __grid_constant__ IsParams p) {
+    extern __shared__ __align__(128) uint8_t stage[];
+    __shared__ int64_t sidx[kIdxInline];
+    __shared__ __align__(8) uint64_t full[4];
+    for (int i = threadIdx.x; i < p.nidx; i += blockDim.x) sidx[i] = p.inl[i];
+    const int64_t* ix = p.nidx ? sidx : p.idx;
+    const int nbuf = p.nbuf;
+    const uint32_t row_bytes = (uint32_t)(p.row_len * (int64_t)sizeof(W));
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < nbuf; ++b) tc::mbar_init(&full[b], 1);
+        tc::fence_barrier_init();
+    }
+    __syncthreads();
+    const uint32_t nmine = (p.nrows - blockIdx.x + gridDim.x - 1) / gridDim.x;
+    auto offsets = [&](uint32_t j, int64_t& offc, int64_t& offa) {
+        uint32_t rem = blockIdx.x + j * gridDim.x;
+        offc = p.off_c;
+        offa = p.off_a;
+        for (int d = 1; d < p.dims.ndim; ++d) {
+            const uint32_t q = d + 1 < p.dims.ndim ? p.dims.div[d].div(rem) : 0;
+            const int64_t k = (int64_t)(rem - q * p.dims.shape[d]);
+            rem = q;
+            offc += k * p.sc[d];
+            offa += (d == p.axis_dim ? ix[k] : k) * p.sa[d];
+        }
+    };
+    auto issue = [&](uint32_t j) {
+        int64_t oc, oa;
+        offsets(j, oc, oa);
+        uint64_t* bar = &full[j % nbuf];
+        const uint8_t* src = reinterpret_cast<const uint8_t*>(a + oa);
+        uint8_t* dst = stage + (size_t)(j % nbuf) * p.buf_stride;
+        tc::mbar_arrive_expect_tx(bar, row_bytes);
+        for (uint32_t o = 0; o < row_bytes; o += kBulkChunk)
+            tc::bulk_load(dst + o, src + o, row_bytes - o < kBulkChunk ? row_bytes - o : kBulkChunk, bar);
+    };
+    if (threadIdx.x == 0)
+        for (uint32_t j = 0; j < (uint32_t)nbuf && j < nmine; ++j) issue(j);
+    const int64_t n0 = p.dims.shape[0], sc0 = p.sc[0];
+    for (uint32_t j = 0; j < nmine; ++j) {
+        const bool ok = tc::mbar_wait(&full[j % nbuf], (j / nbuf) & 1u);
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) {
+                atomicExch(p.err, kIsErrStageWait);
+                for (uint32_t q = j; q < j + (uint32_t)nbuf && q < nmine; ++q)
+                    (void)tc::mbar_wait(&full[q % nbuf], (q / nbuf) & 1u);
+            }
+            return;
+        }
+        int64_t offc, offa;
+        offsets(j, offc, offa);
+        const W* row = reinterpret_cast<const W*>(stage + (size_t)(j % nbuf) * p.buf_stride);
+        for (int64_t k = threadIdx.x; k < n0; k += kBulkThreads) c[offc + k * sc0] = row[ix[k]];
+        __syncthreads();  // every thread is done with this buffer
+        if (threadIdx.x == 0 && j + nbuf < nmine) issue(j + nbuf);
+    }
+}
+
 struct IsDim {
     int64_t shape, sc, sa;
     bool axis;
@@ -91,6 +262,40 @@ struct IsDim {
 
 template <typename W>
 int launch_is(rstsr_ctx* ctx, const IsParams& p, void* c, const void* a) {
+    if (p.nbuf > 0) {
+        const size_t smem = (size_t)p.nbuf * p.buf_stride;
+        static std::atomic<uint64_t> attr_set{0};  // bit d: opted in on device d
+        const uint64_t bit = 1ull << (ctx->device & 63);
+        if (!(attr_set.load() & bit)) {
+            RSTSR_CUDA_TRY(cudaFuncSetAttribute(index_select_bulk_kernel<W>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBulkSmem));
+            attr_set.fetch_or(bit);
+        }
+        const uint32_t cap = (uint32_t)ctx->num_sms;
+        index_select_bulk_kernel<W><<<p.nrows < cap ? p.nrows : cap, kBulkThreads, smem, ctx->stream>>>(
+            static_cast<W*>(c), static_cast<const W*>(a), p);
+        return after_launch(ctx, "index_select_bulk_kernel");
+    }
+    if (p.row_len > 0) {
+        const size_t smem = (size_t)((p.row_len * (int64_t)sizeof(W) + 15) / 16 * 16);
+        static std::atomic<uint64_t> attr_set{0};  // bit d: opted in on device d
+        const uint64_t bit = 1ull << (ctx->device & 63);
+        if (!(attr_set.load() & bit)) {
+            RSTSR_CUDA_TRY(cudaFuncSetAttribute(index_select_staged_kernel<W>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStageMaxBytes));
+            attr_set.fetch_or(bit);
+        }
+        const uint32_t cap = (uint32_t)ctx->num_sms * 2;
+        index_select_staged_kernel<W><<<p.nrows < cap ? p.nrows : cap, kIsThreads, smem, ctx->stream>>>(
+            static_cast<W*>(c), static_cast<const W*>(a), p);
+        return after_launch(ctx, "index_select_staged_kernel");
+    }
+    if (p.nrows > 0) {
+        const uint32_t cap = (uint32_t)ctx->num_sms * 8;
+        index_select_rows_kernel<W><<<p.nrows < cap ? p.nrows : cap, kIsThreads, 0, ctx->stream>>>(
+            static_cast<W*>(c), static_cast<const W*>(a), p);
+        return after_launch(ctx, "index_select_rows_kernel");
+    }
     const int64_t per_cta = (int64_t)kIsThreads * kIsUnroll;
     int64_t grid = (p.total + per_cta - 1) / per_cta;
     const int64_t cap = (int64_t)ctx->num_sms * 8;
@@ -205,8 +410,29 @@ int rstsr_cuda_index_select(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_
         if (merged[d].shape > UINT32_MAX)
             return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "index_select: one collapsed extent above 2^32");
         p.dims.shape[d] = (uint32_t)merged[d].shape;
-        if (!p.big) p.dims.div[d] = FastDiv((uint32_t)merged[d].shape);
+        p.dims.div[d] = FastDiv((uint32_t)merged[d].shape);
     }
+    // rows of the innermost dim when it fills a CTA and the rows count fits
+    if (!merged.empty() && merged[0].shape >= kIsThreads && p.total / merged[0].shape <= INT32_MAX)
+        p.nrows = (uint32_t)(p.total / merged[0].shape);
+    // dense selection along a contiguous innermost source axis: stage the row
+    const int64_t axis_len = La.shape[axis];
+    if (p.nrows > 0 && p.axis_dim == 0 && merged[0].sa == 1 && axis_len * (int64_t)es <= kStageMaxBytes &&
+        nindices * 4 >= axis_len) {
+        p.row_len = axis_len;
+        bool vec_ok = (axis_len * (int64_t)es) % 16 == 0 && reinterpret_cast<uintptr_t>(a) % 16 == 0 &&
+                      (off_a * (int64_t)es) % 16 == 0;
+        for (size_t d = 1; d < merged.size() && vec_ok; ++d)
+            if (!merged[d].axis) vec_ok = (merged[d].sa * (int64_t)es) % 16 == 0;
+        p.stage_vec = vec_ok ? 1 : 0;
+        const int64_t row_bytes = axis_len * (int64_t)es;
+        if (vec_ok && row_bytes >= kBulkMinRow) {
+            p.buf_stride = (uint32_t)((row_bytes + 127) / 128 * 128);
+            const int64_t nb = kBulkSmem / p.buf_stride;
+            p.nbuf = (int)(nb > 4 ? 4 : nb);  // >= 2: rows are at most kStageMaxBytes
+        }
+    }
+    p.err = ctx->dev_err;
     p.off_c = off_c;
     p.off_a = off_a;
 

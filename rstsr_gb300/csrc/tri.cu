@@ -37,8 +37,11 @@ struct TriParams {
     int mirror;              // write the other triangle (symm != N)
     int cols_fast;           // 1: |s_j| <= |s_i|, matrix accesses run along j
     uint32_t tiles;          // tiles along one matrix axis
-    uint64_t pairs;          // tile pairs of one triangle: tiles (tiles + 1) / 2
-    uint64_t total;          // pairs * batches
+    uint32_t pairs;          // tile pairs of one triangle: tiles (tiles + 1) / 2
+    FastDiv div_pairs;
+    uint32_t total;          // pairs * batches
+    uint32_t rows_total;     // n * batches (row kernel)
+    FastDiv div_n;
     int nb;                  // collapsed batch dims (inner first)
     uint32_t bshape[RSTSR_MAX_NDIM];
     FastDiv bdiv[RSTSR_MAX_NDIM];
@@ -52,12 +55,14 @@ __device__ __forceinline__ W sign_bit() {
 }
 
 // Tile pair t -> (P, Q), P >= Q, in the order (0,0), (1,0), (1,1), (2,0), ...
-__device__ __forceinline__ void tri_pair(uint64_t t, uint32_t* P, uint32_t* Q) {
-    uint64_t p = (uint64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (p * (p + 1) / 2 > t) --p;
-    while ((p + 1) * (p + 2) / 2 <= t) ++p;
-    *P = (uint32_t)p;
-    *Q = (uint32_t)(t - p * (p + 1) / 2);
+// The FP32 root is within one of P for t < 2^31 (GB300's FP64 pipe is far too
+// slow to spend per tile); the integer steps make it exact.
+__device__ __forceinline__ void tri_pair(uint32_t t, uint32_t* P, uint32_t* Q) {
+    uint32_t p = (uint32_t)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+    while ((uint64_t)p * (p + 1) / 2 > t) --p;
+    while ((uint64_t)(p + 1) * (p + 2) / 2 <= t) ++p;
+    *P = p;
+    *Q = (uint32_t)(t - (uint64_t)p * (p + 1) / 2);
 }
 
 // First packed index of row i (the element at column j is row_base + j).
@@ -66,22 +71,22 @@ __device__ __forceinline__ int64_t tri_row_base(int64_t i, int64_t n, int lower)
 }
 
 struct TriTile {
-    int64_t R, C;      // tile row / column (in tiles)
+    int32_t R, C;      // tile row / column (in tiles)
     bool diag;
     int64_t mb, pb;    // matrix / packed base offsets of this batch element
 };
 
-__device__ __forceinline__ TriTile tri_tile(const TriParams& p, uint64_t t) {
-    const uint64_t batch = t / p.pairs;
+__device__ __forceinline__ TriTile tri_tile(const TriParams& p, uint32_t t) {
+    const uint32_t batch = p.div_pairs.div(t);
     uint32_t P, Q;
     tri_pair(t - batch * p.pairs, &P, &Q);
     TriTile tt;
-    tt.R = p.lower ? P : Q;
-    tt.C = p.lower ? Q : P;
+    tt.R = (int32_t)(p.lower ? P : Q);
+    tt.C = (int32_t)(p.lower ? Q : P);
     tt.diag = P == Q;
     tt.mb = p.off_m;
     tt.pb = p.off_p;
-    uint32_t b = (uint32_t)batch;
+    uint32_t b = batch;
     for (int d = 0; d < p.nb; ++d) {
         const uint32_t q = p.bdiv[d].div(b);
         const int64_t idx = b - q * p.bshape[d];
@@ -96,80 +101,154 @@ __device__ __forceinline__ bool in_tri(int64_t i, int64_t j, int64_t n, int lowe
     return i < n && j < n && (lower ? j <= i : j >= i);
 }
 
-// Matrix (.., n, n) -> packed (.., n(n+1)/2).
+constexpr int kTriPer = kTriTile / kTriRows;  // rows of a tile per thread
+
+// A tile lies wholly inside the triangle and the matrix: no per-element test.
+__device__ __forceinline__ bool tri_full(const TriParams& p, const TriTile& tt) {
+    return !tt.diag && (int64_t)(tt.R + 1) * kTriTile <= p.n && (int64_t)(tt.C + 1) * kTriTile <= p.n;
+}
+
+// Matrix (.., n, n) -> packed (.., n(n+1)/2), matrix contiguous along j and
+// n >= 64: one warp per matrix row copies the row's part of the triangle,
+// both sides contiguous, four loads in flight per lane, no exchange.
 template <typename W>
-__global__ void __launch_bounds__(kTriTile* kTriRows)
+__global__ void __launch_bounds__(256)
+    pack_tri_rows_kernel(W* __restrict__ packed, const W* __restrict__ mat, const TriParams p) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < p.rows_total; w += nw) {
+        uint32_t b = p.div_n.div(w);
+        const int64_t i = (int64_t)(w - b * (uint32_t)p.n);
+        int64_t mb = p.off_m, pb = p.off_p;
+        for (int d = 0; d < p.nb; ++d) {
+            const uint32_t q = p.bdiv[d].div(b);
+            const int64_t idx = b - q * p.bshape[d];
+            b = q;
+            mb += idx * p.m_bs[d];
+            pb += idx * p.p_bs[d];
+        }
+        const int64_t j0 = p.lower ? 0 : i, j1 = p.lower ? i + 1 : p.n;
+        const W* src = mat + mb + i * p.s_i;
+        W* dst = packed + pb + tri_row_base(i, p.n, p.lower) * p.s_p;
+        for (int64_t j = j0 + lane; j < j1; j += 4 * 32) {
+            W v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j + 32 * u < j1) v[u] = src[(j + 32 * u) * p.s_j];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j + 32 * u < j1) dst[(j + 32 * u) * p.s_p] = v[u];
+        }
+    }
+}
+
+// Matrix -> packed through a shared tile (the matrix is contiguous along i,
+// or n < 64): the shape of the element-wise transpose kernel (32 x 32 tiles,
+// four elements per thread, small register footprint so that eight CTAs share
+// an SM and their loads overlap).
+template <typename W>
+__global__ void __launch_bounds__(kTriTile* kTriRows, 8)
     pack_tri_kernel(W* __restrict__ packed, const W* __restrict__ mat, const TriParams p) {
     __shared__ W tile[kTriTile][kTriTile + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    for (uint64_t t = blockIdx.x; t < p.total; t += gridDim.x) {
+    for (uint32_t t = blockIdx.x; t < p.total; t += gridDim.x) {
         const TriTile tt = tri_tile(p, t);
-        const int64_t i0 = tt.R * kTriTile, j0 = tt.C * kTriTile;
+        const int64_t i0 = (int64_t)tt.R * kTriTile, j0 = (int64_t)tt.C * kTriTile;
+        const bool full = tri_full(p, tt);
 #pragma unroll
-        for (int k = 0; k < kTriTile / kTriRows; ++k) {
+        for (int k = 0; k < kTriPer; ++k) {
             const int a = ty + k * kTriRows;
             const int r = p.cols_fast ? a : tx, c = p.cols_fast ? tx : a;
             const int64_t i = i0 + r, j = j0 + c;
-            if (in_tri(i, j, p.n, p.lower)) tile[r][c] = mat[tt.mb + i * p.s_i + j * p.s_j];
+            if (full || in_tri(i, j, p.n, p.lower)) tile[r][c] = mat[tt.mb + i * p.s_i + j * p.s_j];
         }
         __syncthreads();
 #pragma unroll
-        for (int k = 0; k < kTriTile / kTriRows; ++k) {
+        for (int k = 0; k < kTriPer; ++k) {
             const int r = ty + k * kTriRows, c = tx;
             const int64_t i = i0 + r, j = j0 + c;
-            if (in_tri(i, j, p.n, p.lower))
+            if (full || in_tri(i, j, p.n, p.lower))
                 packed[tt.pb + (tri_row_base(i, p.n, p.lower) + j) * p.s_p] = tile[r][c];
         }
         __syncthreads();
     }
 }
 
-// Packed (.., n(n+1)/2) -> matrix (.., n, n), mirrored by the symmetry.
+// Packed (.., n(n+1)/2) -> matrix (.., n, n), mirrored by the symmetry, in the
+// same transpose-kernel shape: the packed tile is read once into shared
+// memory, then written to its own position and, transposed, to the mirror.
 template <typename W>
-__global__ void __launch_bounds__(kTriTile* kTriRows)
+__global__ void __launch_bounds__(kTriTile* kTriRows, 8)
     unpack_tri_kernel(W* __restrict__ mat, const W* __restrict__ packed, const TriParams p) {
     __shared__ W tile[kTriTile][kTriTile + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const W flip = p.negate ? sign_bit<W>() : W(0);
-    for (uint64_t t = blockIdx.x; t < p.total; t += gridDim.x) {
+    for (uint32_t t = blockIdx.x; t < p.total; t += gridDim.x) {
         const TriTile tt = tri_tile(p, t);
-        const int64_t i0 = tt.R * kTriTile, j0 = tt.C * kTriTile;
+        const int64_t i0 = (int64_t)tt.R * kTriTile, j0 = (int64_t)tt.C * kTriTile;
+        const bool full = tri_full(p, tt);
 #pragma unroll
-        for (int k = 0; k < kTriTile / kTriRows; ++k) {
-            const int r = ty + k * kTriRows, c = tx;
-            const int64_t i = i0 + r, j = j0 + c;
-            if (in_tri(i, j, p.n, p.lower))
-                tile[r][c] = packed[tt.pb + (tri_row_base(i, p.n, p.lower) + j) * p.s_p];
+        for (int k = 0; k < kTriPer; ++k) {
+            const int r = ty + k * kTriRows;
+            const int64_t i = i0 + r, j = j0 + tx;
+            if (full || in_tri(i, j, p.n, p.lower))
+                tile[r][tx] = packed[tt.pb + (tri_row_base(i, p.n, p.lower) + j) * p.s_p];
         }
         __syncthreads();
-        // the tile itself (on a diagonal tile also its mirrored half)
+        W* const mbase = mat + tt.mb;
+        if (full) {
+            // element (i, j) = tile[i - i0][j - j0]; tx runs along the written fast axis
+            {
+                W* dst = p.cols_fast ? mbase + (i0 + ty) * p.s_i + (j0 + tx) * p.s_j
+                                     : mbase + (i0 + tx) * p.s_i + (j0 + ty) * p.s_j;
+                const int64_t step = (int64_t)kTriRows * (p.cols_fast ? p.s_i : p.s_j);
 #pragma unroll
-        for (int k = 0; k < kTriTile / kTriRows; ++k) {
-            const int a = ty + k * kTriRows;
-            const int r = p.cols_fast ? a : tx, c = p.cols_fast ? tx : a;
-            const int64_t i = i0 + r, j = j0 + c;
-            if (i >= p.n || j >= p.n) continue;
-            W v;
-            if (i == j) {
-                v = p.negate ? W(0) : tile[r][c];
-            } else if (in_tri(i, j, p.n, p.lower)) {
-                v = tile[r][c];
-            } else if (p.mirror) {  // diagonal tile only: (j, i) is staged at [c][r]
-                v = tile[c][r] ^ flip;
-            } else {
-                continue;
+                for (int k = 0; k < kTriPer; ++k) {
+                    const int a = ty + k * kTriRows;
+                    *dst = p.cols_fast ? tile[a][tx] : tile[tx][a];
+                    dst += step;
+                }
             }
-            mat[tt.mb + i * p.s_i + j * p.s_j] = v;
-        }
-        if (p.mirror && !tt.diag) {
-            // mirror tile: element (j, i) of the matrix = op(tile[r][c])
+            if (p.mirror) {
+                // element (j, i), at j * s_i + i * s_j, = op(tile[i - i0][j - j0])
+                W* dst = p.cols_fast ? mbase + (j0 + ty) * p.s_i + (i0 + tx) * p.s_j
+                                     : mbase + (j0 + tx) * p.s_i + (i0 + ty) * p.s_j;
+                const int64_t step = (int64_t)kTriRows * (p.cols_fast ? p.s_i : p.s_j);
 #pragma unroll
-            for (int k = 0; k < kTriTile / kTriRows; ++k) {
+                for (int k = 0; k < kTriPer; ++k) {
+                    const int a = ty + k * kTriRows;
+                    *dst = (p.cols_fast ? tile[tx][a] : tile[a][tx]) ^ flip;
+                    dst += step;
+                }
+            }
+        } else {
+            // edge or diagonal tile: per-element tests
+#pragma unroll
+            for (int k = 0; k < kTriPer; ++k) {
                 const int a = ty + k * kTriRows;
-                // along the written matrix's fast axis: its column index is i (= r)
-                const int r = p.cols_fast ? tx : a, c = p.cols_fast ? a : tx;
+                const int r = p.cols_fast ? a : tx, c = p.cols_fast ? tx : a;
                 const int64_t i = i0 + r, j = j0 + c;
-                if (i < p.n && j < p.n) mat[tt.mb + j * p.s_i + i * p.s_j] = tile[r][c] ^ flip;
+                if (i >= p.n || j >= p.n) continue;
+                W w;
+                if (i == j) {
+                    w = p.negate ? W(0) : tile[r][c];
+                } else if (in_tri(i, j, p.n, p.lower)) {
+                    w = tile[r][c];
+                } else if (p.mirror) {  // diagonal tile only: (j, i) is staged at [c][r]
+                    w = tile[c][r] ^ flip;
+                } else {
+                    continue;
+                }
+                mbase[i * p.s_i + j * p.s_j] = w;
+            }
+            if (p.mirror && !tt.diag) {
+#pragma unroll
+                for (int k = 0; k < kTriPer; ++k) {
+                    const int a = ty + k * kTriRows;
+                    const int r = p.cols_fast ? tx : a, c = p.cols_fast ? a : tx;
+                    const int64_t i = i0 + r, j = j0 + c;
+                    if (i < p.n && j < p.n) mbase[j * p.s_i + i * p.s_j] = tile[r][c] ^ flip;
+                }
             }
         }
         __syncthreads();
@@ -218,8 +297,11 @@ int tri_plan(const Layout& lm, const Layout& lp, bool lower, const char* what, T
     p = TriParams{};
     out->empty = sp.size == 0 || n == 0;
     if (out->empty) return RSTSR_OK;
-    if (sp.size > UINT32_MAX)
-        return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, std::string(what) + ": more than 2^32 matrices in the batch");
+    const uint64_t tiles = (uint64_t)((n + kTriTile - 1) / kTriTile);
+    const uint64_t pairs = tiles * (tiles + 1) / 2;
+    if (pairs * (uint64_t)sp.size > INT32_MAX)
+        return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE,
+                    std::string(what) + ": more than 2^31 tiles of 32 x 32 over the batch (split the batch)");
     p.n = n;
     p.s_i = lm.stride[lm.ndim - 2];
     p.s_j = lm.stride[lm.ndim - 1];
@@ -228,9 +310,13 @@ int tri_plan(const Layout& lm, const Layout& lp, bool lower, const char* what, T
     p.off_p = sp.offset[1];
     p.lower = lower ? 1 : 0;
     p.cols_fast = std::llabs(p.s_j) <= std::llabs(p.s_i) ? 1 : 0;
-    p.tiles = (uint32_t)((n + kTriTile - 1) / kTriTile);
-    p.pairs = (uint64_t)p.tiles * (p.tiles + 1) / 2;
-    p.total = p.pairs * (uint64_t)sp.size;
+    p.tiles = (uint32_t)tiles;
+    p.pairs = (uint32_t)pairs;
+    p.div_pairs = FastDiv(p.pairs);
+    p.total = (uint32_t)(pairs * (uint64_t)sp.size);
+    const uint64_t rows_total = (uint64_t)n * (uint64_t)sp.size;
+    p.rows_total = rows_total > INT32_MAX ? 0 : (uint32_t)rows_total;  // 0: row kernel unusable
+    p.div_n = FastDiv((uint32_t)n);
     p.nb = sp.ndim;
     for (int d = 0; d < sp.ndim; ++d) {
         p.bshape[d] = (uint32_t)sp.shape[d];
@@ -241,13 +327,20 @@ int tri_plan(const Layout& lm, const Layout& lp, bool lower, const char* what, T
     return RSTSR_OK;
 }
 
-int tri_grid(rstsr_ctx* ctx, uint64_t total) {
-    const uint64_t cap = (uint64_t)ctx->num_sms * 8;
+int tri_grid(rstsr_ctx* ctx, uint32_t total) {
+    const uint32_t cap = (uint32_t)ctx->num_sms * 16;
     return (int)(total < cap ? total : cap);
 }
 
 template <typename W>
 int launch_pack(rstsr_ctx* ctx, const TriParams& p, void* packed, const void* mat) {
+    if (p.cols_fast && p.n >= 64 && p.rows_total > 0) {
+        const uint32_t warps = p.rows_total, cap = (uint32_t)ctx->num_sms * 64;
+        const uint32_t grid = ((warps < cap ? warps : cap) + 7) / 8;
+        pack_tri_rows_kernel<W><<<grid, 256, 0, ctx->stream>>>(static_cast<W*>(packed),
+                                                               static_cast<const W*>(mat), p);
+        return after_launch(ctx, "pack_tri_rows_kernel");
+    }
     pack_tri_kernel<W><<<tri_grid(ctx, p.total), dim3(kTriTile, kTriRows), 0, ctx->stream>>>(
         static_cast<W*>(packed), static_cast<const W*>(mat), p);
     return after_launch(ctx, "pack_tri_kernel");

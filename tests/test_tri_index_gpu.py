@@ -126,14 +126,15 @@ def test_pack_tri_matches_oracle(cdev, kind, n, batch, uplo):
 @pytest.mark.parametrize("order", ["C", "F"])
 def test_pack_tri_dtypes_and_orders(cdev, dtype, order):
     dev = with_order(cdev, order)
-    shape = (4, 45, 45) if order == "C" else (45, 45, 4)
-    buf = rand(shape, dtype, seed=3).ravel()
-    st = O.c_strides(shape)
-    t = rt.from_host_layout(buf, shape, st, 0, dev)
-    for uplo in ("L", "U"):
-        p = rt.pack_tri(t, uplo)
-        want = oracle_pack(buf, shape, st, 0, uplo == "L", 0 if order == "C" else 1, p.shape, p.stride)
-        np.testing.assert_array_equal(p.to_numpy(), want)
+    for n in (45, 100):  # the shared-tile kernel and the row kernel
+        shape = (4, n, n) if order == "C" else (n, n, 4)
+        buf = rand(shape, dtype, seed=3).ravel()
+        st = O.c_strides(shape)
+        t = rt.from_host_layout(buf, shape, st, 0, dev)
+        for uplo in ("L", "U"):
+            p = rt.pack_tri(t, uplo)
+            want = oracle_pack(buf, shape, st, 0, uplo == "L", 0 if order == "C" else 1, p.shape, p.stride)
+            np.testing.assert_array_equal(p.to_numpy(), want)
 
 
 def test_pack_tri_large_matches_numpy(cdev):
@@ -169,11 +170,12 @@ def bits(dtype):
 @pytest.mark.parametrize("n", [1, 2, 32, 33, 97])
 @pytest.mark.parametrize("kind", ["c", "f", "step2"])
 @pytest.mark.parametrize("uplo", ["L", "U"])
-def test_unpack_tri_matches_oracle(cdev, symm, n, kind, uplo):
+@pytest.mark.parametrize("out_order", ["C", "F"])
+def test_unpack_tri_matches_oracle(cdev, symm, n, kind, uplo, out_order):
     batch = (3,)
     buf, shape, st, off = packed_case(batch, n, np.float64, seed=n, kind=kind)
     t = rt.from_host_layout(buf, shape, st, off, cdev)
-    out = rt.empty(batch + (n, n), np.float64, cdev)
+    out = rt.empty(batch + (n, n), np.float64, cdev, order=out_order)
     rt.fill(out, 7.25)  # the N form must leave the other triangle as it was
     _lib.call("rstsr_cuda_unpack_tri", cdev.ctx, t.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
               C.c_void_p(t.ptr), C.byref(t.layout()), uplo.encode(), rt.tensor.SYMM[symm], 0)
@@ -262,6 +264,44 @@ def test_index_select_matches_oracle(cdev, kind, axis, dtype):
     b = rt.index_select(t, axis, idx)
     want = isel_oracle(buf, shape, st, off, ax, idx, b.shape, b.stride)
     np.testing.assert_array_equal(b.to_numpy(), want)
+
+
+@pytest.mark.parametrize("kind", SEL_KINDS)
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("dtype", [np.float64, np.int16])
+def test_index_select_long_rows_matches_oracle(cdev, kind, axis, dtype):
+    """Innermost extents of a CTA width and more (the row kernel), odd sizes
+    that defeat the vector word, repeated and negative indices."""
+    shape = (5, 300, 301)
+    buf, shape, st, off = sel_case(kind, shape, dtype, seed=8)
+    t = rt.from_host_layout(buf, shape, st, off, cdev)
+    rng = np.random.default_rng(axis + 10)
+    idx = rng.integers(-shape[axis], shape[axis], 300).tolist()
+    b = rt.index_select(t, axis, idx)
+    want = isel_oracle(buf, shape, st, off, axis, idx, b.shape, b.stride)
+    np.testing.assert_array_equal(b.to_numpy(), want)
+
+
+@pytest.mark.parametrize("shape,nidx,dtype,row_step", [
+    ((300, 1024), 600, np.float64, 1),    # 8 KiB rows, four row buffers, inline indices
+    ((64, 12288), 4000, np.float64, 1),   # 96 KiB rows, two row buffers, uploaded indices
+    ((100, 2048), 513, np.float32, 2),    # every other source row
+    ((3, 40, 4096), 1024, np.int16, 1),   # two outer dims
+    ((50, 1001), 700, np.float64, 1),     # row not a multiple of 16 bytes (register staging)
+])
+def test_index_select_dense_columns(cdev, shape, nidx, dtype, row_step):
+    """Dense selections along a contiguous innermost axis (the staged-row
+    kernels: bulk copies into shared memory, or register staging)."""
+    base = list(shape)
+    base[-2] *= row_step
+    a = rand(tuple(base), dtype, seed=nidx)
+    st = list(O.c_strides(base))
+    st[-2] *= row_step
+    view = a[..., ::row_step, :] if row_step > 1 else a
+    t = rt.from_host_layout(a.ravel(), shape, st, 0, cdev)
+    rng = np.random.default_rng(nidx)
+    cols = rng.integers(0, shape[-1], nidx)
+    np.testing.assert_array_equal(rt.index_select(t, len(shape) - 1, cols).to_numpy(), np.take(view, cols, axis=-1))
 
 
 @pytest.mark.parametrize("nidx", [1, 2, 511, 512, 513, 5000])
