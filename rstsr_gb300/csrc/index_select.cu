@@ -31,7 +31,8 @@ constexpr int kIsUnroll = 4;
 constexpr int64_t kStageMaxBytes = 96 * 1024;  // source row staged in shared memory (two CTAs per SM)
 constexpr int kBulkThreads = 512;
 constexpr int64_t kBulkMinRow = 4096;           // rows staged by bulk copies: 4 KiB ..
-constexpr int64_t kBulkSmem = 200 * 1024;       // .. with 2-4 row buffers in this much shared memory
+constexpr int64_t kBulkSmem = 220 * 1024;       // .. with 2-4 row buffers (+ the index list) in this much
+constexpr int64_t kBulkIdxMax = 8192;           // indices kept in shared memory as int32 (else read from global)
 constexpr uint32_t kBulkChunk = 32 * 1024;      // bytes per cp.async.bulk
 constexpr int kIsErrStageWait = 5;              // error word: a staged-row wait gave up
 
@@ -47,6 +48,7 @@ struct IsParams {
     int stage_vec;           // staged kernel: rows load as 16-byte words
     int nbuf;                // bulk kernel: row buffers (0: not the bulk kernel)
     uint32_t buf_stride;     // bulk kernel: bytes between row buffers
+    int idx_smem;            // bulk kernel: the index list is staged in shared memory
     int* err;                // device error word
     int nidx;                // indices held inline (0: use idx)
     const int64_t* idx;      // device copy of the indices (long lists)
@@ -102,7 +104,7 @@ __global__ void __launch_bounds__(kIsThreads)
 // Innermost dim long (>= one CTA width): a CTA walks whole rows of it, the
 // outer multi-index decomposed once per row; four loads in flight per thread.
 template <typename W>
-__global__ void __launch_bounds__(kIsThreads)
+__global__ void __launch_bounds__(kIsThreads, 6)
     index_select_rows_kernel(W* __restrict__ c, const W* __restrict__ a, const __grid_constant__ IsParams p) {
     __shared__ int64_t sidx[kIdxInline];
     for (int i = threadIdx.x; i < p.nidx; i += blockDim.x) sidx[i] = p.inl[i];
@@ -199,12 +201,14 @@ template <typename W>
 __global__ void __launch_bounds__(kBulkThreads)
     index_select_bulk_kernel(W* __restrict__ c, const W* __restrict__ a, const __grid_constant__ IsParams p) {
     extern __shared__ __align__(128) uint8_t stage[];
-    __shared__ int64_t sidx[kIdxInline];
     __shared__ __align__(8) uint64_t full[4];
-    for (int i = threadIdx.x; i < p.nidx; i += blockDim.x) sidx[i] = p.inl[i];
-    const int64_t* ix = p.nidx ? sidx : p.idx;
     const int nbuf = p.nbuf;
+    const int64_t n0 = p.dims.shape[0], sc0 = p.sc[0];
     const uint32_t row_bytes = (uint32_t)(p.row_len * (int64_t)sizeof(W));
+    // the index list as int32 behind the row buffers (indices < row_len <= 96 Ki)
+    int32_t* sidx = reinterpret_cast<int32_t*>(stage + (size_t)nbuf * p.buf_stride);
+    if (p.idx_smem)
+        for (int64_t k = threadIdx.x; k < n0; k += kBulkThreads) sidx[k] = (int32_t)(p.nidx ? p.inl[k] : p.idx[k]);
     if (threadIdx.x == 0) {
         for (int b = 0; b < nbuf; ++b) tc::mbar_init(&full[b], 1);
         tc::fence_barrier_init();
@@ -220,7 +224,7 @@ __global__ void __launch_bounds__(kBulkThreads)
             const int64_t k = (int64_t)(rem - q * p.dims.shape[d]);
             rem = q;
             offc += k * p.sc[d];
-            offa += (d == p.axis_dim ? ix[k] : k) * p.sa[d];
+            offa += k * p.sa[d];  // the indexed axis is dim 0 here
         }
     };
     auto issue = [&](uint32_t j) {
@@ -235,7 +239,6 @@ __global__ void __launch_bounds__(kBulkThreads)
     };
     if (threadIdx.x == 0)
         for (uint32_t j = 0; j < (uint32_t)nbuf && j < nmine; ++j) issue(j);
-    const int64_t n0 = p.dims.shape[0], sc0 = p.sc[0];
     for (uint32_t j = 0; j < nmine; ++j) {
         const bool ok = tc::mbar_wait(&full[j % nbuf], (j / nbuf) & 1u);
         if (!__syncthreads_and(ok)) {
@@ -249,7 +252,19 @@ __global__ void __launch_bounds__(kBulkThreads)
         int64_t offc, offa;
         offsets(j, offc, offa);
         const W* row = reinterpret_cast<const W*>(stage + (size_t)(j % nbuf) * p.buf_stride);
-        for (int64_t k = threadIdx.x; k < n0; k += kBulkThreads) c[offc + k * sc0] = row[ix[k]];
+        for (int64_t k0 = threadIdx.x; k0 < n0; k0 += kBulkThreads * kIsUnroll) {
+            W v[kIsUnroll];
+#pragma unroll
+            for (int u = 0; u < kIsUnroll; ++u) {
+                const int64_t k = k0 + (int64_t)u * kBulkThreads;
+                if (k < n0) v[u] = row[p.idx_smem ? (int64_t)sidx[k] : (p.nidx ? p.inl[k] : p.idx[k])];
+            }
+#pragma unroll
+            for (int u = 0; u < kIsUnroll; ++u) {
+                const int64_t k = k0 + (int64_t)u * kBulkThreads;
+                if (k < n0) c[offc + k * sc0] = v[u];
+            }
+        }
         __syncthreads();  // every thread is done with this buffer
         if (threadIdx.x == 0 && j + nbuf < nmine) issue(j + nbuf);
     }
@@ -263,7 +278,7 @@ struct IsDim {
 template <typename W>
 int launch_is(rstsr_ctx* ctx, const IsParams& p, void* c, const void* a) {
     if (p.nbuf > 0) {
-        const size_t smem = (size_t)p.nbuf * p.buf_stride;
+        const size_t smem = (size_t)p.nbuf * p.buf_stride + (p.idx_smem ? (size_t)p.dims.shape[0] * 4 : 0);
         static std::atomic<uint64_t> attr_set{0};  // bit d: opted in on device d
         const uint64_t bit = 1ull << (ctx->device & 63);
         if (!(attr_set.load() & bit)) {
@@ -291,7 +306,7 @@ int launch_is(rstsr_ctx* ctx, const IsParams& p, void* c, const void* a) {
         return after_launch(ctx, "index_select_staged_kernel");
     }
     if (p.nrows > 0) {
-        const uint32_t cap = (uint32_t)ctx->num_sms * 8;
+        const uint32_t cap = (uint32_t)ctx->num_sms * 6;  // the resident CTAs (40 registers)
         index_select_rows_kernel<W><<<p.nrows < cap ? p.nrows : cap, kIsThreads, 0, ctx->stream>>>(
             static_cast<W*>(c), static_cast<const W*>(a), p);
         return after_launch(ctx, "index_select_rows_kernel");
@@ -428,7 +443,12 @@ int rstsr_cuda_index_select(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_
         const int64_t row_bytes = axis_len * (int64_t)es;
         if (vec_ok && row_bytes >= kBulkMinRow) {
             p.buf_stride = (uint32_t)((row_bytes + 127) / 128 * 128);
-            const int64_t nb = kBulkSmem / p.buf_stride;
+            p.idx_smem = nindices <= kBulkIdxMax ? 1 : 0;
+            int64_t nb = (kBulkSmem - (p.idx_smem ? nindices * 4 : 0)) / p.buf_stride;
+            if (nb < 2 && p.idx_smem) {  // a long row and a long list: keep the list in global memory
+                p.idx_smem = 0;
+                nb = kBulkSmem / p.buf_stride;
+            }
             p.nbuf = (int)(nb > 4 ? 4 : nb);  // >= 2: rows are at most kStageMaxBytes
         }
     }

@@ -288,6 +288,7 @@ def test_index_select_long_rows_matches_oracle(cdev, kind, axis, dtype):
     ((100, 2048), 513, np.float32, 2),    # every other source row
     ((3, 40, 4096), 1024, np.int16, 1),   # two outer dims
     ((50, 1001), 700, np.float64, 1),     # row not a multiple of 16 bytes (register staging)
+    ((20, 16384), 9000, np.float32, 1),   # index list too long for shared memory
 ])
 def test_index_select_dense_columns(cdev, shape, nidx, dtype, row_step):
     """Dense selections along a contiguous innermost axis (the staged-row
