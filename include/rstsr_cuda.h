@@ -431,6 +431,40 @@ int rstsr_cuda_gemm_grouped(rstsr_ctx* ctx, rstsr_dtype t, const rstsr_gemm_prob
 /* Ozaki split statistics of the last f64 GEMM on this thread: slices used. */
 int32_t rstsr_cuda_last_ozaki_slices(void);
 
+/* ------------------------------------------------------ contractions */
+
+/* einsum (crates-plugin/rstsr-tblis/src/einsum_impl.rs:146-199, there through
+ * TBLIS): out = the contraction `subscripts` ("ij,jk->ik"; labels are any
+ * Unicode characters, whitespace ignored, "->" optional with numpy's implicit
+ * output) of the nops operands. Every pairwise contraction runs as one
+ * batched matmul (Ozaki split for F64, bf16 split for F32 unless opts says
+ * otherwise); diagonals are views, single-operand sums use the reduction
+ * kernels. Dtypes F64, F32, I32, I64. lout has the output labels' extents,
+ * any strides. Ellipsis is not supported (RSTSR_ERR_UNIMPLEMENTED). */
+int rstsr_cuda_einsum(rstsr_ctx* ctx, rstsr_dtype t, const char* subscripts, int32_t nops,
+                      const void* const* ops, const rstsr_layout* lops, void* out,
+                      const rstsr_layout* lout, const rstsr_gemm_opts* opts);
+/* Output extents of an einsum (host only). shape_out holds RSTSR_MAX_NDIM. */
+int rstsr_cuda_einsum_output_shape(const char* subscripts, int32_t nops, const rstsr_layout* lops,
+                                   int32_t* ndim_out, int64_t* shape_out);
+
+/* tensordot (crates-plugin/rstsr-tblis/src/tensordot_impl.rs:33-70 with the
+ * labels of rstsr-common/src/tensordot_to_einsum.rs:18-112): c's axes are a's
+ * remaining axes then b's; axes_a[q] of a contracts with axes_b[q] of b
+ * (negative axes count from the end). */
+int rstsr_cuda_tensordot(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc,
+                         const void* a, const rstsr_layout* la, const void* b, const rstsr_layout* lb,
+                         const int64_t* axes_a, const int64_t* axes_b, int32_t naxes,
+                         const rstsr_gemm_opts* opts);
+
+/* DeviceVecdotAPI::vecdot (rstsr-core/src/operators/linalg.rs:3-20; CPU impl
+ * rstsr-native-impl/src/cpu_serial/vecdot.rs): c[m] = sum over the contracted
+ * axes of a[m, s] * b[m, s], the remaining parts of a and b broadcast to c
+ * (for `order`). Real types (no conjugation needed). */
+int rstsr_cuda_vecdot(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc,
+                      const void* a, const rstsr_layout* la, const void* b, const rstsr_layout* lb,
+                      const int64_t* axes_a, const int64_t* axes_b, int32_t naxes, rstsr_order order);
+
 /* ---------------------------------------------------------------- graphs */
 
 /* Capture every call made on the context between begin and end into a CUDA

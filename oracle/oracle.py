@@ -74,9 +74,11 @@ def lib() -> C.CDLL:
         L.oracle_pack_tri.argtypes = [P, LP, P, LP, I, I, I]
         L.oracle_unpack_tri.argtypes = [P, LP, P, LP, I, I, I, I]
         L.oracle_index_select.argtypes = [P, LP, P, LP, I, C.POINTER(C.c_uint64), C.c_int64, I]
+        L.oracle_einsum.argtypes = [I, I, C.POINTER(P), LP, C.POINTER(C.c_int32), P, LP, C.POINTER(C.c_int32), I,
+                                    C.POINTER(C.c_int64)]
         for f in (L.oracle_assign, L.oracle_assign_arbitrary, L.oracle_binary, L.oracle_fma, L.oracle_reduce_axes,
                   L.oracle_argreduce_axes, L.oracle_max_threads, L.oracle_pack_tri, L.oracle_unpack_tri,
-                  L.oracle_index_select):
+                  L.oracle_index_select, L.oracle_einsum):
             f.restype = C.c_int
         _lib = L
     return _lib
@@ -200,3 +202,43 @@ def index_select(dst: Strided, src: Strided, axis: int, indices) -> None:
     _ok(lib().oracle_index_select(_p(dst.buf), C.byref(dst.layout), _p(src.buf), C.byref(src.layout), int(axis),
                                   idx.ctypes.data_as(C.POINTER(C.c_uint64)), C.c_int64(idx.size), dst.buf.itemsize),
         "index_select")
+
+
+def _parse_einsum(subscripts: str, nops: int):
+    """Subscripts -> (input label lists, output labels); numpy's implicit output."""
+    s = "".join(ch for ch in subscripts if not ch.isspace())
+    lhs, arrow, rhs = s.partition("->")
+    ins = lhs.split(",")
+    if len(ins) != nops:
+        raise ValueError("operand count")
+    if not arrow:
+        from collections import Counter
+        cnt = Counter("".join(ins))
+        rhs = "".join(sorted(c for c, n in cnt.items() if n == 1))
+    return ins, rhs
+
+
+def einsum(subscripts: str, *ops: Strided, out: Strided | None = None) -> Strided:
+    """Einstein summation by its definition (f64 with compensated sums, or
+    wrapping i64); ops are Strided f64 or i64 host tensors."""
+    ins, outl = _parse_einsum(subscripts, len(ops))
+    labels = sorted(set("".join(ins)))
+    lid = {c: i for i, c in enumerate(labels)}
+    ext = [0] * len(labels)
+    for sub, t in zip(ins, ops):
+        for c, d in zip(sub, t.shape):
+            ext[lid[c]] = d
+    dt = ops[0].buf.dtype
+    code = 0 if dt == np.float64 else 7
+    if out is None:
+        shape = [ext[lid[c]] for c in outl]
+        out = empty_strided(shape, c_strides(shape), dt)
+    n = len(ops)
+    ptrs = (C.c_void_p * n)(*[t.buf.ctypes.data for t in ops])
+    lays = (OLayout * n)(*[t.layout for t in ops])
+    labs = (C.c_int32 * max(sum(len(x) for x in ins), 1))(*[lid[c] for x in ins for c in x])
+    olabs = (C.c_int32 * max(len(outl), 1))(*[lid[c] for c in outl])
+    exts = (C.c_int64 * max(len(ext), 1))(*ext)
+    _ok(lib().oracle_einsum(code, n, ptrs, lays, labs, _p(out.buf), C.byref(out.layout), olabs, len(labels), exts),
+        "einsum")
+    return out

@@ -20,6 +20,12 @@
  *   unpack_tri        rstsr-native-impl/src/cpu_serial/op_tri.rs:217-410
  *                     (inner_unpack_tri{l,u}_general for Sy/He/Ay/Ah/N)
  *   index_select      rstsr-native-impl/src/cpu_serial/adv_indexing.rs:3-69
+ *   einsum            the definition of an Einstein summation (the reference
+ *                     calls TBLIS 0.2 through crates-plugin/rstsr-tblis/src/
+ *                     einsum_impl.rs:146-199): every output element is the
+ *                     sum, over all values of the labels not in the output,
+ *                     of the product of the operands' elements; f64 with
+ *                     Neumaier-compensated sums, i64 with wrapping arithmetic
  *
  * Every function takes `nthreads`: 1 runs the serial semantics; more threads
  * run the same per-output / per-row algorithm split across OpenMP threads the
@@ -714,6 +720,74 @@ int oracle_index_select(void* c, const olayout* lc, const void* a, const olayout
             oa += (d == axis ? (int64_t)idx[i] : i) * la->stride[d];
         }
         memcpy((char*)c + oc * esize, (const char*)a + oa * esize, (size_t)esize);
+    }
+    return 0;
+}
+
+/* ----------------------------------------------------------- einsum */
+
+/* Labels are ids 0..nlab-1 with extents ext[]; labs holds each operand's
+ * label per axis (ls[k].ndim entries for operand k, concatenated); olabs the
+ * output's. dtype T_F64 or T_I64. */
+int oracle_einsum(int dtype, int nops, const void* const* ops, const olayout* ls, const int32_t* labs, void* out,
+                  const olayout* lo, const int32_t* olabs, int nlab, const int64_t* ext) {
+    if (nlab > 64 || nops > 16) return 1;
+    int is_out[64] = {0};
+    for (int a = 0; a < lo->ndim; ++a) is_out[olabs[a]] = 1;
+    int sum_labs[64], nsum = 0;
+    for (int c = 0; c < nlab; ++c)
+        if (!is_out[c]) sum_labs[nsum++] = c;
+    const int32_t* lab_of[16];
+    int off = 0;
+    for (int k = 0; k < nops; ++k) {
+        lab_of[k] = labs + off;
+        off += ls[k].ndim;
+    }
+    int64_t nsumtot = 1;
+    for (int q = 0; q < nsum; ++q) nsumtot *= ext[sum_labs[q]];
+    const int64_t nout = lsize(lo);
+    int64_t idx[64];
+    for (int64_t e = 0; e < nout; ++e) {
+        /* output label values (C order over the output axes) */
+        int64_t r = e, oo = lo->offset;
+        for (int a = lo->ndim - 1; a >= 0; --a) {
+            idx[olabs[a]] = r % lo->shape[a];
+            r /= lo->shape[a];
+            oo += idx[olabs[a]] * lo->stride[a];
+        }
+        double s = 0.0, comp = 0.0;
+        uint64_t si = 0;
+        for (int64_t q = 0; q < nsumtot; ++q) {
+            int64_t rr = q;
+            for (int t = nsum - 1; t >= 0; --t) {
+                idx[sum_labs[t]] = rr % ext[sum_labs[t]];
+                rr /= ext[sum_labs[t]];
+            }
+            double p = 1.0;
+            uint64_t pi = 1;
+            for (int k = 0; k < nops; ++k) {
+                int64_t o = ls[k].offset;
+                for (int a = 0; a < ls[k].ndim; ++a) o += idx[lab_of[k][a]] * ls[k].stride[a];
+                if (dtype == T_F64)
+                    p *= ((const double*)ops[k])[o];
+                else
+                    pi *= (uint64_t)((const int64_t*)ops[k])[o];
+            }
+            if (dtype == T_F64) { /* Neumaier */
+                const double t2 = s + p;
+                if (fabs(s) >= fabs(p))
+                    comp += (s - t2) + p;
+                else
+                    comp += (p - t2) + s;
+                s = t2;
+            } else {
+                si += pi;
+            }
+        }
+        if (dtype == T_F64)
+            ((double*)out)[oo] = s + comp;
+        else
+            ((int64_t*)out)[oo] = (int64_t)si;
     }
     return 0;
 }

@@ -24,6 +24,7 @@ from .tensor import (  # noqa: F401
     binary_inplace,
     binary_scalar,
     bool_select,
+    einsum,
     empty,
     fill,
     fma,
@@ -37,9 +38,11 @@ from .tensor import (  # noqa: F401
     reduce_axes,
     reduce_axes_into,
     take,
+    tensordot,
     to_contig,
     unary,
     unpack_tri,
+    vecdot,
     zeros,
 )
 

@@ -178,6 +178,16 @@ _SIGS = {
         [_P, _I, _P, _L, _P, _L, C.c_int32, C.POINTER(C.c_uint64), C.c_int64],
         C.c_int,
     ),
+    "rstsr_cuda_einsum": ([_P, _I, C.c_char_p, _I, C.POINTER(_P), _L, _P, _L, C.POINTER(GemmOpts)], C.c_int),
+    "rstsr_cuda_einsum_output_shape": ([C.c_char_p, _I, _L, C.POINTER(C.c_int32), C.POINTER(C.c_int64)], C.c_int),
+    "rstsr_cuda_tensordot": (
+        [_P, _I, _P, _L, _P, _L, _P, _L, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _I, C.POINTER(GemmOpts)],
+        C.c_int,
+    ),
+    "rstsr_cuda_vecdot": (
+        [_P, _I, _P, _L, _P, _L, _P, _L, C.POINTER(C.c_int64), C.POINTER(C.c_int64), _I, _I],
+        C.c_int,
+    ),
     "rstsr_cuda_gemm": (
         [_P, _I, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_int64, C.c_double, _P, C.c_int64, _P, C.c_int64,
          C.c_double, _P, C.c_int64, _I, C.POINTER(GemmOpts)],

@@ -1,0 +1,699 @@
+// einsum / tensordot / vecdot on the device.
+//
+// The reference contracts through TBLIS (crates-plugin/rstsr-tblis/src/
+// einsum_impl.rs:146-199, tensordot_impl.rs:33-58 with the subscript builder
+// rstsr-common/src/tensordot_to_einsum.rs:18-112; TBLIS 0.2 and
+// opt-einsum-path 0.2 are third-party and not vendored), and vecdot through
+// rstsr-native-impl/src/cpu_serial/vecdot.rs (DeviceVecdotAPI,
+// rstsr-core/src/operators/linalg.rs:3-20).
+//
+// Here a host planner turns an einsum into calls of this library's own
+// kernels, with the tensor cores doing every contraction:
+//   1. repeated labels in one operand become a diagonal view (the strides of
+//      the repeated axes add up; no copy);
+//   2. labels that occur in one operand only and not in the output are summed
+//      out with the reduction kernels;
+//   3. while two or more operands remain, the pair whose result is smallest
+//      (ties: the larger contraction) is contracted: labels split into batch
+//      (both operands, kept), contracted (both, not kept) and free (one
+//      operand, kept); the operands are viewed as [batch, M, K] x [batch, K, N]
+//      when their axes merge (else copied contiguous first) and multiplied by
+//      one batched matmul launch (Ozaki split for f64, bf16 split for f32);
+//      with nothing contracted the product is the broadcast multiply kernel;
+//   4. the last operand is permuted into the output by the copy kernels,
+//      unless the last contraction could write the output directly.
+// Labels are Unicode code points (the reference's own example uses Greek
+// letters); whitespace is ignored; "->" is optional (implicit output: the
+// labels seen once, in code-point order, as numpy does).
+#include <algorithm>
+#include <map>
+#include <set>
+
+#include "ew_kernel.cuh"
+
+namespace rstsr {
+
+namespace {
+
+struct EinOp {
+    const void* ptr = nullptr;
+    Layout l;
+    std::vector<int> lab;
+    void* owned = nullptr;  // intermediate storage of this operand (freed when consumed)
+};
+
+// UTF-8 to code points; returns false on a malformed sequence.
+bool utf8_decode(const char* s, std::vector<int>& out) {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(s);
+    while (*p) {
+        int c = *p, n = 0;
+        if (c < 0x80) {
+            n = 0;
+        } else if ((c & 0xE0) == 0xC0) {
+            c &= 0x1F;
+            n = 1;
+        } else if ((c & 0xF0) == 0xE0) {
+            c &= 0x0F;
+            n = 2;
+        } else if ((c & 0xF8) == 0xF0) {
+            c &= 0x07;
+            n = 3;
+        } else {
+            return false;
+        }
+        ++p;
+        for (int k = 0; k < n; ++k, ++p) {
+            if ((*p & 0xC0) != 0x80) return false;
+            c = (c << 6) | (*p & 0x3F);
+        }
+        out.push_back(c);
+    }
+    return true;
+}
+
+bool is_space(int c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r'; }
+
+// "ij,jk->ik": input label lists and the output list.
+int parse_subscripts(const char* subscripts, int nops, std::vector<std::vector<int>>& ins, std::vector<int>& out) {
+    if (!subscripts) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: null subscripts");
+    std::vector<int> cps;
+    if (!utf8_decode(subscripts, cps)) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: subscripts are not UTF-8");
+    ins.assign(1, {});
+    bool arrow = false;
+    for (size_t i = 0; i < cps.size(); ++i) {
+        const int c = cps[i];
+        if (is_space(c)) continue;
+        if (c == '.') return fail(RSTSR_ERR_UNIMPLEMENTED, "einsum: ellipsis broadcasting is not supported");
+        if (c == '-') {
+            if (i + 1 >= cps.size() || cps[i + 1] != '>' || arrow)
+                return fail(RSTSR_ERR_INVALID_VALUE, "einsum: malformed '->' in subscripts");
+            arrow = true;
+            ++i;
+            continue;
+        }
+        if (c == ',') {
+            if (arrow) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: ',' after '->'");
+            ins.emplace_back();
+            continue;
+        }
+        if (c == '>') return fail(RSTSR_ERR_INVALID_VALUE, "einsum: stray '>' in subscripts");
+        if (arrow)
+            out.push_back(c);
+        else
+            ins.back().push_back(c);
+    }
+    if ((int)ins.size() != nops)
+        return fail(RSTSR_ERR_INVALID_VALUE, "einsum: " + std::to_string(ins.size()) + " subscript groups for " +
+                                                 std::to_string(nops) + " operands");
+    if (!arrow) {
+        std::map<int, int> count;
+        for (auto& v : ins)
+            for (int c : v) count[c]++;
+        for (auto& kv : count)
+            if (kv.second == 1) out.push_back(kv.first);  // std::map: code-point order
+    }
+    std::set<int> seen;
+    for (int c : out)
+        if (!seen.insert(c).second) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: an output label repeats");
+    std::set<int> all;
+    for (auto& v : ins) all.insert(v.begin(), v.end());
+    for (int c : out)
+        if (!all.count(c)) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: an output label is in no operand");
+    return RSTSR_OK;
+}
+
+// Extent of every label, checked consistent across operands.
+int label_extents(const std::vector<std::vector<int>>& ins, const std::vector<Layout>& ls, std::map<int, int64_t>& ext) {
+    for (size_t k = 0; k < ins.size(); ++k) {
+        if ((int)ins[k].size() != ls[k].ndim)
+            return fail(RSTSR_ERR_INVALID_LAYOUT, "einsum: operand " + std::to_string(k) + " has " +
+                                                      std::to_string(ls[k].ndim) + " axes but " +
+                                                      std::to_string(ins[k].size()) + " labels");
+        for (size_t a = 0; a < ins[k].size(); ++a) {
+            auto it = ext.find(ins[k][a]);
+            if (it == ext.end())
+                ext[ins[k][a]] = ls[k].shape[a];
+            else if (it->second != ls[k].shape[a])
+                return fail(RSTSR_ERR_INVALID_LAYOUT, "einsum: a label has extents " + std::to_string(it->second) +
+                                                          " and " + std::to_string(ls[k].shape[a]));
+        }
+    }
+    return RSTSR_OK;
+}
+
+// Merge a repeated label into one axis (the diagonal view).
+void take_diagonals(EinOp& op) {
+    std::vector<int> lab;
+    Layout l;
+    l.offset = op.l.offset;
+    for (int a = 0; a < op.l.ndim; ++a) {
+        auto it = std::find(lab.begin(), lab.end(), op.lab[a]);
+        if (it == lab.end()) {
+            lab.push_back(op.lab[a]);
+            l.shape[l.ndim] = op.l.shape[a];
+            l.stride[l.ndim] = op.l.stride[a];
+            l.ndim++;
+        } else {
+            l.stride[it - lab.begin()] += op.l.stride[a];
+        }
+    }
+    op.l = l;
+    op.lab = lab;
+}
+
+void release(rstsr_ctx* ctx, EinOp& op) {
+    if (op.owned) scratch_free(ctx, op.owned);
+    op.owned = nullptr;
+}
+
+int64_t prod_ext(const std::vector<int>& labs, const std::map<int, int64_t>& ext) {
+    int64_t p = 1;
+    for (int c : labs) p *= ext.at(c);
+    return p;
+}
+
+// Sum out the axes whose labels are not in `keep`.
+int sum_unkept(rstsr_ctx* ctx, rstsr_dtype t, EinOp& op, const std::set<int>& keep) {
+    std::vector<int64_t> axes;
+    std::vector<int> lab;
+    for (int a = 0; a < op.l.ndim; ++a) {
+        if (keep.count(op.lab[a]))
+            lab.push_back(op.lab[a]);
+        else
+            axes.push_back(a);
+    }
+    if (axes.empty()) return RSTSR_OK;
+    // the kept axes, C-contiguous, in their current order
+    std::vector<int64_t> kshape;
+    for (int a = 0; a < op.l.ndim; ++a)
+        if (keep.count(op.lab[a])) kshape.push_back(op.l.shape[a]);
+    Layout lo = Layout::c_contig(kshape.data(), (int)kshape.size());
+    const int64_t n = std::max<int64_t>(lo.size(), 1);
+    void* buf = nullptr;
+    RSTSR_TRY(scratch_alloc(ctx, (size_t)n * dtype_size(t), &buf));
+    rstsr_layout la = op.l.to_abi(), lab_o = lo.to_abi();
+    int rc = rstsr_cuda_reduce_axes_into(ctx, RSTSR_RED_SUM, t, op.ptr, &la, axes.data(), (int32_t)axes.size(), buf,
+                                         &lab_o);
+    if (rc != RSTSR_OK) {
+        scratch_free(ctx, buf);
+        return rc;
+    }
+    release(ctx, op);
+    op.ptr = buf;
+    op.owned = buf;
+    op.l = lo;
+    op.lab = lab;
+    return RSTSR_OK;
+}
+
+// View the axes `axes` (in this order) of l as one axis; false if they do not
+// merge. Extent-1 axes never block a merge; no axes gives extent 1.
+bool merge_axes(const Layout& l, const std::vector<int>& axes, int64_t* ext, int64_t* stride) {
+    int64_t e = 1, s = 1;
+    bool have = false;
+    for (int k = (int)axes.size() - 1; k >= 0; --k) {  // innermost last in the list
+        const int a = axes[k];
+        if (l.shape[a] == 1) continue;
+        if (!have) {
+            s = l.stride[a];
+            e = l.shape[a];
+            have = true;
+        } else {
+            if (l.stride[a] != s * e) return false;
+            e *= l.shape[a];
+        }
+    }
+    *ext = e;
+    *stride = s;
+    return true;
+}
+
+// Copy op into C-contiguous scratch with its axes permuted to `order`.
+int make_contig(rstsr_ctx* ctx, rstsr_dtype t, EinOp& op, const std::vector<int>& order) {
+    Layout src;
+    src.ndim = (int)order.size();
+    src.offset = op.l.offset;
+    std::vector<int64_t> shp;
+    std::vector<int> lab;
+    for (size_t k = 0; k < order.size(); ++k) {
+        src.shape[k] = op.l.shape[order[k]];
+        src.stride[k] = op.l.stride[order[k]];
+        shp.push_back(src.shape[k]);
+        lab.push_back(op.lab[order[k]]);
+    }
+    Layout dst = Layout::c_contig(shp.data(), (int)shp.size());
+    const int64_t n = std::max<int64_t>(dst.size(), 1);
+    void* buf = nullptr;
+    RSTSR_TRY(scratch_alloc(ctx, (size_t)n * dtype_size(t), &buf));
+    rstsr_layout ld = dst.to_abi(), ls = src.to_abi();
+    int rc = rstsr_cuda_assign(ctx, buf, &ld, t, op.ptr, &ls, t);
+    if (rc != RSTSR_OK) {
+        scratch_free(ctx, buf);
+        return rc;
+    }
+    release(ctx, op);
+    op.ptr = buf;
+    op.owned = buf;
+    op.l = dst;
+    op.lab = lab;
+    return RSTSR_OK;
+}
+
+// [g0, g1, g2] groups of axes of op as a 3-D view; copies op contiguous (in the
+// group order) when a group does not merge.
+int view3(rstsr_ctx* ctx, rstsr_dtype t, EinOp& op, const std::vector<int>* groups_lab, Layout* v) {
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        v->ndim = 3;
+        v->offset = op.l.offset;
+        bool ok = true;
+        for (int g = 0; g < 3 && ok; ++g) {
+            std::vector<int> axes;
+            for (int c : groups_lab[g]) axes.push_back((int)(std::find(op.lab.begin(), op.lab.end(), c) - op.lab.begin()));
+            ok = merge_axes(op.l, axes, &v->shape[g], &v->stride[g]);
+        }
+        if (ok) return RSTSR_OK;
+        std::vector<int> order;
+        for (int g = 0; g < 3; ++g)
+            for (int c : groups_lab[g]) order.push_back((int)(std::find(op.lab.begin(), op.lab.end(), c) - op.lab.begin()));
+        RSTSR_TRY(make_contig(ctx, t, op, order));
+    }
+    return fail(RSTSR_ERR_RUNTIME, "einsum: contiguous operand did not merge");
+}
+
+// Contract A and B over their shared labels not in `keep`. The result's labels
+// are batch, free(A), free(B) in the order given by `pref` (labels listed
+// there first, in that order). When `out` is given and its layout merges into
+// [batch, M, N] for that label order, the product is written there directly.
+int contract_pair(rstsr_ctx* ctx, rstsr_dtype t, EinOp& A, EinOp& B, const std::set<int>& keep,
+                  const std::map<int, int64_t>& ext, const std::vector<int>& pref, const rstsr_gemm_opts* opts,
+                  EinOp* res, void* out, const Layout* lout, const std::vector<int>* out_lab, bool* wrote_out) {
+    *wrote_out = false;
+    std::vector<int> batch, con, fa, fb;
+    for (int c : A.lab) {
+        const bool inb = std::find(B.lab.begin(), B.lab.end(), c) != B.lab.end();
+        if (inb && keep.count(c))
+            batch.push_back(c);
+        else if (inb)
+            con.push_back(c);
+        else
+            fa.push_back(c);
+    }
+    for (int c : B.lab)
+        if (std::find(A.lab.begin(), A.lab.end(), c) == A.lab.end()) fb.push_back(c);
+    auto by_pref = [&](std::vector<int>& v) {
+        std::stable_sort(v.begin(), v.end(), [&](int x, int y) {
+            auto px = std::find(pref.begin(), pref.end(), x), py = std::find(pref.begin(), pref.end(), y);
+            return px < py;
+        });
+    };
+    by_pref(batch);
+    by_pref(fa);
+    by_pref(fb);
+    std::vector<int> rlab = batch;
+    rlab.insert(rlab.end(), fa.begin(), fa.end());
+    rlab.insert(rlab.end(), fb.begin(), fb.end());
+    if ((int)rlab.size() > RSTSR_MAX_NDIM)
+        return fail(RSTSR_ERR_UNIMPLEMENTED, "einsum: an intermediate would have more than 8 axes");
+    const int64_t nb = prod_ext(batch, ext), m = prod_ext(fa, ext), n = prod_ext(fb, ext), k = prod_ext(con, ext);
+
+    // destination: the output itself when the label order matches and it merges
+    Layout lc;
+    void* cptr = nullptr;
+    void* owned = nullptr;
+    if (out && out_lab && *out_lab == rlab) {
+        std::vector<int> g[3];
+        for (size_t i = 0; i < rlab.size(); ++i)
+            g[i < batch.size() ? 0 : (i < batch.size() + fa.size() ? 1 : 2)].push_back((int)i);
+        lc.ndim = 3;
+        lc.offset = lout->offset;
+        bool ok = true;
+        for (int q = 0; q < 3 && ok; ++q) ok = merge_axes(*lout, g[q], &lc.shape[q], &lc.stride[q]);
+        if (ok) {
+            cptr = out;
+            *wrote_out = true;
+        }
+    }
+    if (!cptr) {
+        const int64_t shp[3] = {nb, m, n};
+        lc = Layout::c_contig(shp, 3);
+        RSTSR_TRY(scratch_alloc(ctx, (size_t)std::max<int64_t>(nb * m * n, 1) * dtype_size(t), &owned));
+        cptr = owned;
+    }
+    auto fail_free = [&](int rc) {
+        if (owned) scratch_free(ctx, owned);
+        *wrote_out = false;
+        return rc;
+    };
+    int rc = RSTSR_OK;
+    if (nb * m * n == 0) {
+        // nothing to write
+    } else if (k == 0) {
+        rstsr_layout l = lc.to_abi();
+        const double zero = 0.0;
+        const float zf = 0.0f;
+        const int64_t zi = 0;
+        const void* z = t == RSTSR_F64 ? (const void*)&zero : t == RSTSR_F32 ? (const void*)&zf : (const void*)&zi;
+        rc = rstsr_cuda_fill(ctx, cptr, &l, t, z);
+    } else if (con.empty()) {
+        // outer product per batch: c[b, i, j] = a[b, i] * b[b, j] (broadcast multiply)
+        Layout va, vb;
+        const std::vector<int> ga[3] = {batch, fa, {}}, gb[3] = {batch, {}, fb};
+        rc = view3(ctx, t, A, ga, &va);
+        if (rc == RSTSR_OK) rc = view3(ctx, t, B, gb, &vb);
+        if (rc != RSTSR_OK) return fail_free(rc);
+        Layout xa = lc, xb = lc;
+        xa.offset = va.offset;
+        xa.stride[0] = va.stride[0];
+        xa.stride[1] = va.stride[1];
+        xa.stride[2] = 0;
+        xb.offset = vb.offset;
+        xb.stride[0] = vb.stride[0];
+        xb.stride[1] = 0;
+        xb.stride[2] = vb.stride[2];
+        if (nb == 1) xa.stride[0] = xb.stride[0] = 0;
+        rstsr_layout l0 = lc.to_abi(), l1 = xa.to_abi(), l2 = xb.to_abi();
+        rc = rstsr_cuda_binary(ctx, RSTSR_OP_MUL, t, cptr, &l0, A.ptr, &l1, B.ptr, &l2);
+    } else {
+        Layout va, vb;
+        const std::vector<int> ga[3] = {batch, fa, con}, gb[3] = {batch, con, fb};
+        rc = view3(ctx, t, A, ga, &va);
+        if (rc == RSTSR_OK) rc = view3(ctx, t, B, gb, &vb);
+        if (rc != RSTSR_OK) return fail_free(rc);
+        rstsr_layout l0, l1, l2;
+        if (nb == 1) {  // a plain GEMM on the [M, K] x [K, N] views
+            Layout c2 = lc, a2 = va, b2 = vb;
+            c2.ndim = a2.ndim = b2.ndim = 2;
+            for (int q = 0; q < 2; ++q) {
+                c2.shape[q] = lc.shape[q + 1];
+                c2.stride[q] = lc.stride[q + 1];
+                a2.shape[q] = va.shape[q + 1];
+                a2.stride[q] = va.stride[q + 1];
+                b2.shape[q] = vb.shape[q + 1];
+                b2.stride[q] = vb.stride[q + 1];
+            }
+            l0 = c2.to_abi();
+            l1 = a2.to_abi();
+            l2 = b2.to_abi();
+        } else {
+            l0 = lc.to_abi();
+            l1 = va.to_abi();
+            l2 = vb.to_abi();
+        }
+        rc = rstsr_cuda_matmul(ctx, t, cptr, &l0, A.ptr, &l1, B.ptr, &l2, 1.0, 0.0, RSTSR_ROW_MAJOR, opts);
+    }
+    if (rc != RSTSR_OK) return fail_free(rc);
+    release(ctx, A);
+    release(ctx, B);
+    if (!*wrote_out) {
+        std::vector<int64_t> shp;
+        for (int c : rlab) shp.push_back(ext.at(c));
+        res->l = Layout::c_contig(shp.data(), (int)shp.size());
+        res->ptr = cptr;
+        res->owned = owned;
+        res->lab = rlab;
+    }
+    return RSTSR_OK;
+}
+
+bool einsum_dtype_ok(rstsr_dtype t) {
+    return t == RSTSR_F64 || t == RSTSR_F32 || t == RSTSR_I32 || t == RSTSR_I64;
+}
+
+int einsum_impl(rstsr_ctx* ctx, rstsr_dtype t, const std::vector<std::vector<int>>& ins, const std::vector<int>& olab,
+                int nops, const void* const* ptrs, const std::vector<Layout>& ls, void* out, const Layout& lout,
+                const rstsr_gemm_opts* opts) {
+    std::map<int, int64_t> ext;
+    RSTSR_TRY(label_extents(ins, ls, ext));
+    if (lout.ndim != (int)olab.size())
+        return fail(RSTSR_ERR_INVALID_LAYOUT, "einsum: the output has " + std::to_string(lout.ndim) + " axes for " +
+                                                  std::to_string(olab.size()) + " output labels");
+    for (size_t a = 0; a < olab.size(); ++a)
+        if (lout.shape[a] != ext[olab[a]])
+            return fail(RSTSR_ERR_INVALID_LAYOUT, "einsum: output extent differs from the label's");
+    RSTSR_TRY(check_write_layout(lout, "einsum"));
+    if (lout.size() == 0) return RSTSR_OK;
+    for (int k = 0; k < nops; ++k)
+        if (!ptrs[k] && ls[k].size() > 0) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: null operand pointer");
+    if (!out) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: null output pointer");
+
+    std::vector<EinOp> ops(nops);
+    for (int k = 0; k < nops; ++k) {
+        ops[k].ptr = ptrs[k];
+        ops[k].l = ls[k];
+        ops[k].lab = ins[k];
+        take_diagonals(ops[k]);
+    }
+    const std::set<int> oset(olab.begin(), olab.end());
+    auto keep_for = [&](size_t self, size_t other) {
+        std::set<int> keep = oset;
+        for (size_t q = 0; q < ops.size(); ++q)
+            if (q != self && q != other) keep.insert(ops[q].lab.begin(), ops[q].lab.end());
+        return keep;
+    };
+    auto cleanup = [&](int rc) {
+        for (auto& o : ops) release(ctx, o);
+        return rc;
+    };
+    // 2. labels of one operand only
+    for (size_t k = 0; k < ops.size(); ++k) {
+        std::set<int> keep = keep_for(k, k);
+        int rc = sum_unkept(ctx, t, ops[k], keep);
+        if (rc != RSTSR_OK) return cleanup(rc);
+    }
+    // 3. pairwise contractions, smallest result first
+    while (ops.size() > 1) {
+        size_t bi = 0, bj = 1;
+        int64_t best_size = -1, best_k = 0;
+        for (size_t i = 0; i < ops.size(); ++i)
+            for (size_t j = i + 1; j < ops.size(); ++j) {
+                const std::set<int> keep = keep_for(i, j);
+                std::set<int> rl;
+                int64_t kk = 1;
+                for (int c : ops[i].lab) {
+                    const bool inb = std::find(ops[j].lab.begin(), ops[j].lab.end(), c) != ops[j].lab.end();
+                    if (!inb || keep.count(c))
+                        rl.insert(c);
+                    else
+                        kk *= ext[c];
+                }
+                for (int c : ops[j].lab) rl.insert(c);
+                for (auto it = rl.begin(); it != rl.end();)
+                    it = (!keep.count(*it) && std::find(ops[i].lab.begin(), ops[i].lab.end(), *it) != ops[i].lab.end() &&
+                          std::find(ops[j].lab.begin(), ops[j].lab.end(), *it) != ops[j].lab.end())
+                             ? rl.erase(it)
+                             : std::next(it);
+                int64_t sz = 1;
+                for (int c : rl) sz *= ext[c];
+                if (best_size < 0 || sz < best_size || (sz == best_size && kk > best_k)) {
+                    best_size = sz;
+                    best_k = kk;
+                    bi = i;
+                    bj = j;
+                }
+            }
+        const std::set<int> keep = keep_for(bi, bj);
+        const bool last = ops.size() == 2;
+        // the last contraction: let the output order decide which operand is A
+        if (last) {
+            auto first_free = [&](const EinOp& x, const EinOp& y) {
+                for (int c : olab) {
+                    const bool inx = std::find(x.lab.begin(), x.lab.end(), c) != x.lab.end();
+                    const bool iny = std::find(y.lab.begin(), y.lab.end(), c) != y.lab.end();
+                    if (inx && !iny) return 0;
+                    if (iny && !inx) return 1;
+                }
+                return 0;
+            };
+            if (first_free(ops[bi], ops[bj]) == 1) std::swap(bi, bj);
+        }
+        EinOp res;
+        bool wrote = false;
+        int rc = contract_pair(ctx, t, ops[bi], ops[bj], keep, ext, olab, opts, &res, last ? out : nullptr,
+                               last ? &lout : nullptr, last ? &olab : nullptr, &wrote);
+        if (rc != RSTSR_OK) return cleanup(rc);
+        const size_t hi = std::max(bi, bj), lo = std::min(bi, bj);
+        ops.erase(ops.begin() + hi);
+        ops.erase(ops.begin() + lo);
+        if (wrote) return cleanup(RSTSR_OK);
+        ops.push_back(res);
+    }
+    // 4. permute the last operand into the output
+    EinOp& f = ops[0];
+    int rc = sum_unkept(ctx, t, f, oset);
+    if (rc != RSTSR_OK) return cleanup(rc);
+    Layout src;
+    src.ndim = (int)olab.size();
+    src.offset = f.l.offset;
+    for (size_t a = 0; a < olab.size(); ++a) {
+        const int ax = (int)(std::find(f.lab.begin(), f.lab.end(), olab[a]) - f.lab.begin());
+        src.shape[a] = f.l.shape[ax];
+        src.stride[a] = f.l.stride[ax];
+    }
+    rstsr_layout lo = lout.to_abi(), lsrc = src.to_abi();
+    rc = rstsr_cuda_assign(ctx, out, &lo, t, f.ptr, &lsrc, t);
+    return cleanup(rc);
+}
+
+int read_layouts(int nops, const rstsr_layout* lops, std::vector<Layout>& ls) {
+    if (nops < 1) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: at least one operand is required");
+    if (!lops) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: null layouts");
+    for (int k = 0; k < nops; ++k) {
+        RSTSR_TRY(check_layout(&lops[k], "operand"));
+        ls.push_back(Layout::from_abi(lops[k]));
+    }
+    return RSTSR_OK;
+}
+
+// Labels of tensordot (rstsr-common/src/tensordot_to_einsum.rs:18-112):
+// contracted pairs first, then A's remaining axes, then B's; the output keeps
+// A's free axes then B's.
+int tensordot_labels(int nda, int ndb, const int64_t* axes_a, const int64_t* axes_b, int naxes,
+                     std::vector<std::vector<int>>& ins, std::vector<int>& out) {
+    if (naxes < 0 || naxes > nda || naxes > ndb)
+        return fail(RSTSR_ERR_INVALID_LAYOUT, "tensordot: more contracted axes than dimensions");
+    std::vector<int> la(nda, -1), lb(ndb, -1);
+    int next = 'a';
+    for (int q = 0; q < naxes; ++q) {
+        int64_t x = axes_a[q] < 0 ? axes_a[q] + nda : axes_a[q];
+        int64_t y = axes_b[q] < 0 ? axes_b[q] + ndb : axes_b[q];
+        if (x < 0 || x >= nda || y < 0 || y >= ndb) return fail(RSTSR_ERR_AXIS, "tensordot: axis out of range");
+        if (la[x] >= 0 || lb[y] >= 0) return fail(RSTSR_ERR_INVALID_VALUE, "tensordot: an axis repeats");
+        la[x] = lb[y] = next++;
+    }
+    for (int i = 0; i < nda; ++i)
+        if (la[i] < 0) {
+            la[i] = next++;
+            out.push_back(la[i]);
+        }
+    for (int j = 0; j < ndb; ++j)
+        if (lb[j] < 0) {
+            lb[j] = next++;
+            out.push_back(lb[j]);
+        }
+    ins = {la, lb};
+    return RSTSR_OK;
+}
+
+}  // namespace
+
+}  // namespace rstsr
+
+using namespace rstsr;
+
+extern "C" {
+
+int rstsr_cuda_einsum_output_shape(const char* subscripts, int32_t nops, const rstsr_layout* lops,
+                                   int32_t* ndim_out, int64_t* shape_out) {
+    clear_error();
+    std::vector<Layout> ls;
+    RSTSR_TRY(read_layouts(nops, lops, ls));
+    std::vector<std::vector<int>> ins;
+    std::vector<int> olab;
+    RSTSR_TRY(parse_subscripts(subscripts, nops, ins, olab));
+    std::map<int, int64_t> ext;
+    RSTSR_TRY(label_extents(ins, ls, ext));
+    if ((int)olab.size() > RSTSR_MAX_NDIM) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: output has too many axes");
+    if (!ndim_out || !shape_out) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: null output arguments");
+    *ndim_out = (int32_t)olab.size();
+    for (size_t a = 0; a < olab.size(); ++a) shape_out[a] = ext[olab[a]];
+    return RSTSR_OK;
+}
+
+int rstsr_cuda_einsum(rstsr_ctx* ctx, rstsr_dtype t, const char* subscripts, int32_t nops, const void* const* ops,
+                      const rstsr_layout* lops, void* out, const rstsr_layout* lout, const rstsr_gemm_opts* opts) {
+    clear_error();
+    RSTSR_TRY(enter(ctx));
+    if (!einsum_dtype_ok(t))
+        return fail(RSTSR_ERR_INVALID_VALUE, std::string("einsum: unsupported element type ") + dtype_name(t));
+    std::vector<Layout> ls;
+    RSTSR_TRY(read_layouts(nops, lops, ls));
+    RSTSR_TRY(check_layout(lout, "out"));
+    if (!ops) return fail(RSTSR_ERR_INVALID_VALUE, "einsum: null operand list");
+    std::vector<std::vector<int>> ins;
+    std::vector<int> olab;
+    RSTSR_TRY(parse_subscripts(subscripts, nops, ins, olab));
+    return einsum_impl(ctx, t, ins, olab, nops, ops, ls, out, Layout::from_abi(*lout), opts);
+}
+
+int rstsr_cuda_tensordot(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc, const void* a,
+                         const rstsr_layout* la, const void* b, const rstsr_layout* lb, const int64_t* axes_a,
+                         const int64_t* axes_b, int32_t naxes, const rstsr_gemm_opts* opts) {
+    clear_error();
+    RSTSR_TRY(enter(ctx));
+    if (!einsum_dtype_ok(t))
+        return fail(RSTSR_ERR_INVALID_VALUE, std::string("tensordot: unsupported element type ") + dtype_name(t));
+    RSTSR_TRY(check_layout(lc, "c"));
+    RSTSR_TRY(check_layout(la, "a"));
+    RSTSR_TRY(check_layout(lb, "b"));
+    if (naxes > 0 && (!axes_a || !axes_b)) return fail(RSTSR_ERR_INVALID_VALUE, "tensordot: null axes");
+    std::vector<Layout> ls = {Layout::from_abi(*la), Layout::from_abi(*lb)};
+    std::vector<std::vector<int>> ins;
+    std::vector<int> olab;
+    RSTSR_TRY(tensordot_labels(ls[0].ndim, ls[1].ndim, axes_a, axes_b, naxes, ins, olab));
+    const void* ptrs[2] = {a, b};
+    return einsum_impl(ctx, t, ins, olab, 2, ptrs, ls, c, Layout::from_abi(*lc), opts);
+}
+
+int rstsr_cuda_vecdot(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc, const void* a,
+                      const rstsr_layout* la, const void* b, const rstsr_layout* lb, const int64_t* axes_a,
+                      const int64_t* axes_b, int32_t naxes, rstsr_order order) {
+    clear_error();
+    RSTSR_TRY(enter(ctx));
+    RSTSR_TRY(check_layout(lc, "c"));
+    RSTSR_TRY(check_layout(la, "a"));
+    RSTSR_TRY(check_layout(lb, "b"));
+    if (!dtype_valid(t) || t == RSTSR_BOOL) return fail(RSTSR_ERR_INVALID_VALUE, "vecdot: unsupported dtype");
+    if (naxes < 1 || !axes_a || !axes_b) return fail(RSTSR_ERR_INVALID_VALUE, "vecdot: no contracted axes");
+    Layout A = Layout::from_abi(*la), B = Layout::from_abi(*lb), Cl = Layout::from_abi(*lc);
+    Layout as, am, bs, bm;
+    Error err;
+    std::vector<int> norm_a, norm_b;
+    if (!split_axes(A, axes_a, naxes, &as, &am, &norm_a, &err) || !split_axes(B, axes_b, naxes, &bs, &bm, &norm_b, &err))
+        return fail(err.code, "vecdot: " + err.msg);
+    if (!same_shape(as, bs))
+        return fail(RSTSR_ERR_INVALID_LAYOUT,
+                    "vecdot: the dimensions of a and b along the contracted axes should be the same");
+    // remaining parts broadcast to c (broadcast_layout_to_first, cpu_serial/vecdot.rs:37-40)
+    Layout cb, amb, bmb;
+    if (!broadcast_layouts(Cl, am, order, &cb, &amb, &err) || !same_shape(cb, Cl) ||
+        !broadcast_layouts(Cl, bm, order, &cb, &bmb, &err) || !same_shape(cb, Cl))
+        return fail(RSTSR_ERR_INVALID_LAYOUT, "vecdot: a and b do not broadcast to c after the axis sum");
+    RSTSR_TRY(check_write_layout(Cl, "vecdot"));
+    if (Cl.size() == 0) return RSTSR_OK;
+    // product over [c's axes..., contracted axes...] then the sum over the contracted axes
+    Layout P, PA, PB;
+    P.ndim = PA.ndim = PB.ndim = Cl.ndim + as.ndim;
+    if (P.ndim > RSTSR_MAX_NDIM) return fail(RSTSR_ERR_INVALID_LAYOUT, "vecdot: too many axes");
+    std::vector<int64_t> pshape;
+    for (int d = 0; d < Cl.ndim; ++d) pshape.push_back(Cl.shape[d]);
+    for (int d = 0; d < as.ndim; ++d) pshape.push_back(as.shape[d]);
+    P = Layout::c_contig(pshape.data(), (int)pshape.size());
+    PA.offset = amb.offset;
+    PB.offset = bmb.offset;
+    for (int d = 0; d < Cl.ndim; ++d) {
+        PA.shape[d] = PB.shape[d] = Cl.shape[d];
+        PA.stride[d] = amb.stride[d];
+        PB.stride[d] = bmb.stride[d];
+    }
+    for (int d = 0; d < as.ndim; ++d) {
+        PA.shape[Cl.ndim + d] = PB.shape[Cl.ndim + d] = as.shape[d];
+        PA.stride[Cl.ndim + d] = as.stride[d];
+        PB.stride[Cl.ndim + d] = bs.stride[d];
+    }
+    PA.offset += as.offset - A.offset;  // split_axes keeps the offset on both parts
+    PB.offset += bs.offset - B.offset;
+    const int64_t n = std::max<int64_t>(P.size(), 1);
+    void* buf = nullptr;
+    RSTSR_TRY(scratch_alloc(ctx, (size_t)n * dtype_size(t), &buf));
+    rstsr_layout l0 = P.to_abi(), l1 = PA.to_abi(), l2 = PB.to_abi();
+    int rc = rstsr_cuda_binary(ctx, RSTSR_OP_MUL, t, buf, &l0, a, &l1, b, &l2);
+    if (rc == RSTSR_OK) {
+        std::vector<int64_t> axes;
+        for (int d = 0; d < as.ndim; ++d) axes.push_back(Cl.ndim + d);
+        rc = rstsr_cuda_reduce_axes_into(ctx, RSTSR_RED_SUM, t, buf, &l0, axes.data(), (int32_t)axes.size(), c, lc);
+    }
+    scratch_free(ctx, buf);
+    return rc;
+}
+
+}  // extern "C"

@@ -915,3 +915,118 @@ Tensor.unpack_triu = lambda self, symm="Sy": unpack_tri(self, "U", symm)
 Tensor.index_select = index_select
 Tensor.take = lambda self, indices, axis: take(self, indices, axis)
 Tensor.bool_select = bool_select
+
+
+# ------------------------------------------------------------ contractions
+
+
+def _gemm_opts(precision: int, slices: int):
+    opts = _lib.GemmOpts()
+    opts.precision = precision
+    opts.ozaki_slices = slices
+    return opts
+
+
+def _contig_out(shape, dtype_code: int, device: DeviceCuda) -> Tensor:
+    return empty(shape, dtype_code, device, order="C" if device.default_order == ROW_MAJOR else "F")
+
+
+def einsum(subscripts: str, *operands: Tensor, precision: int = 0, slices: int = 0) -> Tensor:
+    """einsum (crates-plugin/rstsr-tblis/src/einsum_impl.rs:146-199): the
+    output is contiguous in the device's default order."""
+    if not operands:
+        raise RstsrError(2, "at least one operand is required")
+    dev = operands[0].device
+    for t in operands[1:]:
+        if not t.device.same_device(dev):
+            raise RstsrError(2, "all operands must be on the same device")
+        if t.dtype_code != operands[0].dtype_code:
+            raise RstsrError(2, "einsum operands must share one dtype")
+    n = len(operands)
+    lays = (Layout * n)(*[t.layout() for t in operands])
+    nd = C.c_int32()
+    shp = (C.c_int64 * _lib.MAX_NDIM)()
+    sub = subscripts.encode("utf-8")
+    call("rstsr_cuda_einsum_output_shape", sub, n, lays, C.byref(nd), shp)
+    out = _contig_out(tuple(shp[i] for i in range(nd.value)), operands[0].dtype_code, dev)
+    ptrs = (C.c_void_p * n)(*[t.ptr for t in operands])
+    opts = _gemm_opts(precision, slices)
+    call("rstsr_cuda_einsum", dev.ctx, operands[0].dtype_code, sub, n, ptrs, lays, C.c_void_p(out.ptr),
+         C.byref(out.layout()), C.byref(opts))
+    return out
+
+
+def _axes_pair(axes, nda: int, ndb: int):
+    if axes is None:
+        axes = 2
+    if isinstance(axes, numbers.Integral):
+        n = int(axes)
+        if n < 0:
+            raise RstsrError(2, "n must be non-negative")
+        if n > nda or n > ndb:
+            raise RstsrError(1, "n must be less than or equal to the number of dimensions of both tensors")
+        return list(range(nda - n, nda)), list(range(n))
+    xa, xb = axes
+    xa = [int(xa)] if isinstance(xa, numbers.Integral) else [int(x) for x in xa]
+    xb = [int(xb)] if isinstance(xb, numbers.Integral) else [int(x) for x in xb]
+    if len(xa) != len(xb):
+        raise RstsrError(2, "axes_a and axes_b should have the same length")
+    return xa, xb
+
+
+def tensordot(a: Tensor, b: Tensor, axes=2, precision: int = 0, slices: int = 0) -> Tensor:
+    """tensordot (crates-plugin/rstsr-tblis/src/tensordot_impl.rs:60-70):
+    `axes` is n (last n axes of a with the first n of b) or (axes_a, axes_b)."""
+    _same_device(a, b)
+    xa, xb = _axes_pair(axes, a.ndim, b.ndim)
+    na = [x % a.ndim if a.ndim else x for x in xa]
+    nb = [x % b.ndim if b.ndim else x for x in xb]
+    shape = tuple(a.shape[i] for i in range(a.ndim) if i not in na) + \
+        tuple(b.shape[j] for j in range(b.ndim) if j not in nb)
+    out = _contig_out(shape, a.dtype_code, a.device)
+    ka = (C.c_int64 * max(len(xa), 1))(*xa)
+    kb = (C.c_int64 * max(len(xb), 1))(*xb)
+    opts = _gemm_opts(precision, slices)
+    call("rstsr_cuda_tensordot", a.device.ctx, a.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
+         C.c_void_p(a.ptr), C.byref(a.layout()), C.c_void_p(b.ptr), C.byref(b.layout()), ka, kb, len(xa),
+         C.byref(opts))
+    return out
+
+
+def vecdot(a: Tensor, b: Tensor, axes=None) -> Tensor:
+    """vecdot_f (rstsr-core/src/tensor/linalg/vecdot.rs:160-247): dot products
+    along `axes` (default the last axis; an int counts from the end of each
+    operand when negative), the remaining parts broadcast against each other."""
+    _same_device(a, b)
+    if axes is None:
+        axes = -1
+    if isinstance(axes, numbers.Integral):
+        ax = int(axes)
+        mn = min(a.ndim, b.ndim)
+        if ax < 0:
+            if not -mn <= ax <= -1:
+                raise RstsrError(2, "axis should be [-N, -1] where N is min(a.ndim, b.ndim)")
+            xa, xb = [ax + a.ndim], [ax + b.ndim]
+        else:
+            if not 0 <= ax < mn:
+                raise RstsrError(2, "axis should be [0, N) where N is min(a.ndim, b.ndim)")
+            xa, xb = [ax], [ax]
+    else:
+        xa, xb = _axes_pair(axes, a.ndim, b.ndim)
+        xa = [x % a.ndim for x in xa]
+        xb = [x % b.ndim for x in xb]
+    order = a.device.default_order
+    ra = a._view(tuple(a.shape[i] for i in range(a.ndim) if i not in xa),
+                 tuple(a.stride[i] for i in range(a.ndim) if i not in xa), a.offset)
+    rb = b._view(tuple(b.shape[i] for i in range(b.ndim) if i not in xb),
+                 tuple(b.stride[i] for i in range(b.ndim) if i not in xb), b.offset)
+    oa, ob = broadcast_layouts(ra, rb, order)
+    lc = Layout()
+    call("rstsr_cuda_layout_binary_op", C.byref(oa), C.byref(ob), order, C.byref(lc))
+    _, hi = _bounds(lc.shape_t, lc.stride_t, lc.offset)
+    out = Tensor(Storage(a.device, max(hi, 1) * a.itemsize), lc.shape_t, lc.stride_t, lc.offset, a.dtype_code)
+    ka = (C.c_int64 * len(xa))(*xa)
+    kb = (C.c_int64 * len(xb))(*xb)
+    call("rstsr_cuda_vecdot", a.device.ctx, a.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
+         C.c_void_p(a.ptr), C.byref(a.layout()), C.c_void_p(b.ptr), C.byref(b.layout()), ka, kb, len(xa), order)
+    return out

@@ -211,6 +211,26 @@ TRI_INDEX_CASES = [
 ]
 
 
+# Contractions: tensordot (through TBLIS in the reference) and vecdot.
+CONTRACTION_CASES = [
+    dict(src="crates-plugin/rstsr-tblis/src/tensordot_impl.rs:81-92", op="tensordot", dtype="f64",
+         a=[[1.0, 2.0], [3.0, 4.0]], b=[[5.0, 6.0], [7.0, 8.0]], axes=0,
+         expect=[[[[5, 6], [7, 8]], [[10, 12], [14, 16]]], [[[15, 18], [21, 24]], [[20, 24], [28, 32]]]]),
+    dict(src="crates-plugin/rstsr-tblis/src/tensordot_impl.rs:94-105", op="tensordot", dtype="f64",
+         a_arange=60, a_shape=[3, 4, 5], b_arange=24, b_shape=[4, 3, 2], axes=[[1, 0], [0, 1]],
+         expect=[[4400.0, 4730.0], [4532.0, 4874.0], [4664.0, 5018.0], [4796.0, 5162.0], [4928.0, 5306.0]]),
+    dict(src="rstsr-core/src/tensor/linalg/vecdot.rs:418-424", op="vecdot", dtype="i64",
+         a_arange=[0, 6], a_shape=[2, 3], b_arange=[6, 12], b_shape=[2, 3], expect=[23, 122]),
+    dict(src="rstsr-core/src/tensor/linalg/vecdot.rs:426-430", op="vecdot", dtype="f64",
+         a=[[0.0, 5.0, 0.0], [0.0, 0.0, 10.0], [0.0, 6.0, 8.0]], b=[0.0, 0.6, 0.8], expect=[3.0, 8.0, 10.0],
+         tol=1e-12),
+    dict(src="rstsr-core/tests/doc_draft/linalg/test_vecdot.rs:18-23", op="vecdot", dtype="i32",
+         a=[1, 2, 3], b=[4, 5, 6], expect=32),
+    dict(src="rstsr-core/tests/doc_draft/linalg/test_vecdot.rs:25-32", op="vecdot", dtype="i32",
+         a=[[1, 2], [3, 4]], b=[[5, 6], [7, 8]], expect=[17, 53]),
+]
+
+
 def main() -> None:
     here = Path(__file__).resolve().parent
     out = here / "reference_kats.json"
@@ -219,6 +239,9 @@ def main() -> None:
     out = here / "tri_index_kats.json"
     out.write_text(json.dumps(TRI_INDEX_CASES, indent=1) + "\n")
     print(f"wrote {len(TRI_INDEX_CASES)} cases to {out}")
+    out = here / "contraction_kats.json"
+    out.write_text(json.dumps(CONTRACTION_CASES, indent=1) + "\n")
+    print(f"wrote {len(CONTRACTION_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
