@@ -394,6 +394,7 @@ def run_gpu(args):
             result["gemm"].update(run_batched_section(dev, stream))
             result["small_f64"] = run_small_section(dev, stream)
             result["tri_index"] = run_tri_index_section(dev, stream)
+            result["contraction"] = run_contraction_section(dev, stream)
         if not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline(args)
     if world > 1:
@@ -799,6 +800,84 @@ def run_tri_index_section(dev, stream, n=2048, batch=32, rows=16384, cols=8192):
     return out
 
 
+def run_contraction_section(dev, stream, P=1000, nao=350, nocc=50, nvir=300, vec_rows=8192, vec_cols=8192):
+    """The 3-index AO -> MO transform B[P, i, a] = sum_mn B[P, m, n] Co[m, i] Cv[n, a]
+    (f64, synthetic seeded inputs; P = 1000, nao = 350, nocc = 50, nvir = 300:
+    the B[1000, 50, 300] that the Ozaki SYRK then contracts), through einsum:
+    two batched split GEMMs (2*P*nao*nao*nocc + 2*P*nocc*nao*nvir flop), against
+    torch.einsum in FP64 (cuBLAS DGEMM) on the same data and the relative
+    Frobenius error against that FP64 result; plus vecdot of two
+    [vec_rows, vec_cols] f64 arrays along the last axis (HBM-bound: 2 reads)."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    out = {}
+    rng = np.random.default_rng(0)
+    B = rng.standard_normal((P, nao, nao)) * np.exp(-0.01 * np.arange(P))[:, None, None]
+    Co = rng.standard_normal((nao, nocc))
+    Cv = rng.standard_normal((nao, nvir))
+    tB, tCo, tCv = rt.asarray(B, dev), rt.asarray(Co, dev), rt.asarray(Cv, dev)
+    gB, gCo, gCv = torch.from_numpy(B).cuda(), torch.from_numpy(Co).cuda(), torch.from_numpy(Cv).cuda()
+    del B
+    sub = "Pmn,mi,na->Pia"
+    l0 = dev.launch_count()
+    res = rt.einsum(sub, tB, tCo, tCv)
+    torch.cuda.synchronize()
+    launches = dev.launch_count() - l0
+    sec = _time_events(stream, lambda: rt.einsum(sub, tB, tCo, tCv), 5)
+    ref = torch.einsum("Pmn,mi->Pin", gB, gCo)
+    ref = torch.einsum("Pin,na->Pia", ref, gCv)
+    sec_t = _time_events(stream, lambda: torch.einsum("Pin,na->Pia", torch.einsum("Pmn,mi->Pin", gB, gCo), gCv), 2)
+    got = torch.as_tensor(res.to_numpy()).cuda()
+    err = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
+    flops = 2.0 * P * nao * nao * nocc + 2.0 * P * nocc * nao * nvir
+    out["einsum_3index_f64"] = {
+        "subscripts": sub, "shapes": [[P, nao, nao], [nao, nocc], [nao, nvir]],
+        "tflops": round(flops / sec / 1e12, 2), "ms": round(sec * 1e3, 3), "flop": flops,
+        "rel_err_frobenius_vs_fp64": err, "launches_per_call": int(launches),
+        "torch_fp64_tflops": round(flops / sec_t / 1e12, 3), "torch_fp64_ms": round(sec_t * 1e3, 3)}
+    # host sample: numpy einsum (BLAS) on P = 32 of the 1000 (scaled by P)
+    import time as _t
+    Bs = rng.standard_normal((32, nao, nao))
+    t0 = _t.perf_counter()
+    np.einsum(sub, Bs, Co, Cv, optimize=True)
+    host = _t.perf_counter() - t0
+    out["einsum_3index_f64"]["cpu_numpy_sample"] = {"P": 32, "s": round(host, 4),
+                                                   "tflops": round(flops * 32 / P / host / 1e12, 4)}
+    del tB, gB, ref, got, res
+    torch.cuda.empty_cache()
+    a = rng.standard_normal((vec_rows, vec_cols))
+    b = rng.standard_normal((vec_rows, vec_cols))
+    ta, tb = rt.asarray(a, dev), rt.asarray(b, dev)
+    l0 = dev.launch_count()
+    v = rt.vecdot(ta, tb)
+    torch.cuda.synchronize()
+    launches = dev.launch_count() - l0
+    sec = _time_events(stream, lambda: rt.vecdot(ta, tb), 5)
+    want = np.einsum("ij,ij->i", a, b)
+    nbytes = 2 * vec_rows * vec_cols * 8 + vec_rows * 8
+    out["vecdot_f64"] = {"shape": [vec_rows, vec_cols], "gbs": round(nbytes / sec / 1e9, 1), "ms": round(sec * 1e3, 4),
+                         "launches_per_call": int(launches),
+                         "max_rel_err": float(np.max(np.abs(v.to_numpy() - want)) / np.max(np.abs(want)))}
+    del ta, tb
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_contraction_only(args):
+    """Only the contraction section (profiling)."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    dev = rt.DeviceCuda(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev.set_stream(stream.cuda_stream)
+    return {"section": "contraction", "results": run_contraction_section(dev, stream, P=args.ein_p)}
+
+
 def run_tri_index_only(args):
     """Only the packed-triangle / index-selection section (profiling)."""
     import torch
@@ -1008,8 +1087,10 @@ def main():
     # restrict the workload (profiling a small case): comma-separated subsets
     ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
-    ap.add_argument("--only", default="", choices=["", "c3", "tri_index"],
-                    help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select")
+    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction"],
+                    help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select; "
+                         "contraction: only einsum / vecdot")
+    ap.add_argument("--ein-p", type=int, default=1000, help="P of the 3-index transform for --only contraction")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
     ap.add_argument("--tri-batch", type=int, default=32, help="matrices for --only tri_index")
@@ -1020,6 +1101,8 @@ def main():
         res = run_c3_only(args)
     elif args.only == "tri_index":
         res = run_tri_index_only(args)
+    elif args.only == "contraction":
+        res = run_contraction_only(args)
     elif args.impl == "reference":
         res = run_reference(args)
     else:

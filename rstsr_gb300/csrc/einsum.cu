@@ -259,84 +259,137 @@ int make_contig(rstsr_ctx* ctx, rstsr_dtype t, EinOp& op, const std::vector<int>
     return RSTSR_OK;
 }
 
-// [g0, g1, g2] groups of axes of op as a 3-D view; copies op contiguous (in the
-// group order) when a group does not merge.
-int view3(rstsr_ctx* ctx, rstsr_dtype t, EinOp& op, const std::vector<int>* groups_lab, Layout* v) {
-    for (int attempt = 0; attempt < 2; ++attempt) {
-        v->ndim = 3;
-        v->offset = op.l.offset;
-        bool ok = true;
-        for (int g = 0; g < 3 && ok; ++g) {
-            std::vector<int> axes;
-            for (int c : groups_lab[g]) axes.push_back((int)(std::find(op.lab.begin(), op.lab.end(), c) - op.lab.begin()));
-            ok = merge_axes(op.l, axes, &v->shape[g], &v->stride[g]);
-        }
-        if (ok) return RSTSR_OK;
-        std::vector<int> order;
-        for (int g = 0; g < 3; ++g)
-            for (int c : groups_lab[g]) order.push_back((int)(std::find(op.lab.begin(), op.lab.end(), c) - op.lab.begin()));
-        RSTSR_TRY(make_contig(ctx, t, op, order));
-    }
-    return fail(RSTSR_ERR_RUNTIME, "einsum: contiguous operand did not merge");
+int axis_of(const EinOp& op, int c) { return (int)(std::find(op.lab.begin(), op.lab.end(), c) - op.lab.begin()); }
+
+bool has(const std::vector<int>& v, int c) { return std::find(v.begin(), v.end(), c) != v.end(); }
+
+// Merge the axes of `op` carrying `labs` (outer to inner).
+bool merge_labels(const EinOp& op, const std::vector<int>& labs, int64_t* e, int64_t* st) {
+    std::vector<int> axes;
+    for (int c : labs) axes.push_back(axis_of(op, c));
+    return merge_axes(op.l, axes, e, st);
 }
 
-// Contract A and B over their shared labels not in `keep`. The result's labels
-// are batch, free(A), free(B) in the order given by `pref` (labels listed
-// there first, in that order). When `out` is given and its layout merges into
-// [batch, M, N] for that label order, the product is written there directly.
+// Labels ordered by decreasing |stride| in op (outer first; extent-1 last).
+std::vector<int> by_stride(const EinOp& op, std::vector<int> labs) {
+    std::stable_sort(labs.begin(), labs.end(), [&](int x, int y) {
+        const int ax = axis_of(op, x), ay = axis_of(op, y);
+        const bool ux = op.l.shape[ax] == 1, uy = op.l.shape[ay] == 1;
+        if (ux != uy) return uy;
+        return std::llabs(op.l.stride[ax]) > std::llabs(op.l.stride[ay]);
+    });
+    return labs;
+}
+
+// The longest inner run of `labs` (ordered by stride) that merges in op; the
+// labels before it are returned in `moved` (they become batch axes).
+std::vector<int> merged_suffix(const EinOp& op, const std::vector<int>& labs, std::vector<int>* moved) {
+    moved->clear();
+    for (size_t cut = 0; cut < labs.size(); ++cut) {
+        std::vector<int> tail(labs.begin() + cut, labs.end());
+        int64_t e, st;
+        if (merge_labels(op, tail, &e, &st)) {
+            moved->assign(labs.begin(), labs.begin() + cut);
+            return tail;
+        }
+    }
+    return {};
+}
+
+// Contract A and B over their shared labels not in `keep` with one batched
+// matmul. Matmul views: A as [batch..., M, K], B as [batch..., K, N], the
+// batch axes being the labels both keep plus free labels whose axes do not
+// merge into M (or N) -- those get stride 0 in the other operand, so that the
+// matmul broadcasts instead of a copy. K's labels are ordered so that they
+// merge in both operands; an operand is copied contiguous only when no order
+// works. The result's labels are batch, M's, N's. When `out` is given and its
+// layout fits that label order, the product is written there directly.
 int contract_pair(rstsr_ctx* ctx, rstsr_dtype t, EinOp& A, EinOp& B, const std::set<int>& keep,
                   const std::map<int, int64_t>& ext, const std::vector<int>& pref, const rstsr_gemm_opts* opts,
                   EinOp* res, void* out, const Layout* lout, const std::vector<int>* out_lab, bool* wrote_out) {
     *wrote_out = false;
     std::vector<int> batch, con, fa, fb;
     for (int c : A.lab) {
-        const bool inb = std::find(B.lab.begin(), B.lab.end(), c) != B.lab.end();
-        if (inb && keep.count(c))
+        if (has(B.lab, c) && keep.count(c))
             batch.push_back(c);
-        else if (inb)
+        else if (has(B.lab, c))
             con.push_back(c);
         else
             fa.push_back(c);
     }
     for (int c : B.lab)
-        if (std::find(A.lab.begin(), A.lab.end(), c) == A.lab.end()) fb.push_back(c);
+        if (!has(A.lab, c)) fb.push_back(c);
     auto by_pref = [&](std::vector<int>& v) {
         std::stable_sort(v.begin(), v.end(), [&](int x, int y) {
-            auto px = std::find(pref.begin(), pref.end(), x), py = std::find(pref.begin(), pref.end(), y);
-            return px < py;
+            return std::find(pref.begin(), pref.end(), x) < std::find(pref.begin(), pref.end(), y);
         });
     };
     by_pref(batch);
     by_pref(fa);
     by_pref(fb);
-    std::vector<int> rlab = batch;
-    rlab.insert(rlab.end(), fa.begin(), fa.end());
-    rlab.insert(rlab.end(), fb.begin(), fb.end());
-    if ((int)rlab.size() > RSTSR_MAX_NDIM)
-        return fail(RSTSR_ERR_UNIMPLEMENTED, "einsum: an intermediate would have more than 8 axes");
-    const int64_t nb = prod_ext(batch, ext), m = prod_ext(fa, ext), n = prod_ext(fb, ext), k = prod_ext(con, ext);
+    const int64_t k = prod_ext(con, ext);
 
-    // destination: the output itself when the label order matches and it merges
-    Layout lc;
-    void* cptr = nullptr;
-    void* owned = nullptr;
-    if (out && out_lab && *out_lab == rlab) {
-        std::vector<int> g[3];
-        for (size_t i = 0; i < rlab.size(); ++i)
-            g[i < batch.size() ? 0 : (i < batch.size() + fa.size() ? 1 : 2)].push_back((int)i);
-        lc.ndim = 3;
-        lc.offset = lout->offset;
-        bool ok = true;
-        for (int q = 0; q < 3 && ok; ++q) ok = merge_axes(*lout, g[q], &lc.shape[q], &lc.stride[q]);
-        if (ok) {
-            cptr = out;
-            *wrote_out = true;
+    // the labels of the matmul axes
+    std::vector<int> mlab, klab, nlab, movedA, movedB;
+    if (!con.empty()) {
+        auto k_ok = [&](const std::vector<int>& ord) {
+            int64_t e, st;
+            return merge_labels(A, ord, &e, &st) && merge_labels(B, ord, &e, &st);
+        };
+        // copy X contiguous as [batch, free, K] (A) or [batch, K, free] (B)
+        auto copy_operand = [&](bool is_a) {
+            EinOp& X = is_a ? A : B;
+            std::vector<int> order;
+            for (int c : batch) order.push_back(axis_of(X, c));
+            if (is_a) {
+                for (int c : fa) order.push_back(axis_of(X, c));
+                for (int c : klab) order.push_back(axis_of(X, c));
+            } else {
+                for (int c : klab) order.push_back(axis_of(X, c));
+                for (int c : fb) order.push_back(axis_of(X, c));
+            }
+            return make_contig(ctx, t, X, order);
+        };
+        klab = by_stride(A, con);
+        if (!k_ok(klab)) {
+            klab = by_stride(B, con);
+            if (!k_ok(klab)) {
+                // copy the smaller operand with K in the other's order; the other too if needed
+                const bool copy_a = A.l.size() <= B.l.size();
+                klab = by_stride(copy_a ? B : A, con);
+                RSTSR_TRY(copy_operand(copy_a));
+                if (!k_ok(klab)) RSTSR_TRY(copy_operand(!copy_a));
+            }
         }
+        mlab = fa.empty() ? fa : merged_suffix(A, by_stride(A, fa), &movedA);
+        nlab = fb.empty() ? fb : merged_suffix(B, by_stride(B, fb), &movedB);
+    } else {
+        mlab = fa;
+        nlab = fb;
     }
-    if (!cptr) {
-        const int64_t shp[3] = {nb, m, n};
-        lc = Layout::c_contig(shp, 3);
-        RSTSR_TRY(scratch_alloc(ctx, (size_t)std::max<int64_t>(nb * m * n, 1) * dtype_size(t), &owned));
+    std::vector<int> bl = batch;
+    bl.insert(bl.end(), movedA.begin(), movedA.end());
+    bl.insert(bl.end(), movedB.begin(), movedB.end());
+    std::vector<int> rlab = bl;
+    rlab.insert(rlab.end(), mlab.begin(), mlab.end());
+    rlab.insert(rlab.end(), nlab.begin(), nlab.end());
+    if ((int)rlab.size() > RSTSR_MAX_NDIM || (int)bl.size() + 2 > RSTSR_MAX_NDIM)
+        return fail(RSTSR_ERR_UNIMPLEMENTED, "einsum: an intermediate would have more than 8 axes");
+    const int64_t nres = prod_ext(rlab, ext);
+
+    // the product's destination: the output itself when its axes fit, else scratch
+    void* owned = nullptr;
+    void* cptr = nullptr;
+    Layout lres;  // result over rlab
+    if (out && out_lab && *out_lab == rlab) {
+        cptr = out;
+        lres = *lout;
+        *wrote_out = true;
+    } else {
+        std::vector<int64_t> shp;
+        for (int c : rlab) shp.push_back(ext.at(c));
+        lres = Layout::c_contig(shp.data(), (int)shp.size());
+        RSTSR_TRY(scratch_alloc(ctx, (size_t)std::max<int64_t>(nres, 1) * dtype_size(t), &owned));
         cptr = owned;
     }
     auto fail_free = [&](int rc) {
@@ -344,70 +397,90 @@ int contract_pair(rstsr_ctx* ctx, rstsr_dtype t, EinOp& A, EinOp& B, const std::
         *wrote_out = false;
         return rc;
     };
+    // a view of X over `labs` (stride 0 for labels X lacks)
+    auto view_over = [&](const EinOp& X, const std::vector<int>& labs) {
+        Layout v;
+        v.ndim = (int)labs.size();
+        v.offset = X.l.offset;
+        for (size_t q = 0; q < labs.size(); ++q) {
+            v.shape[q] = ext.at(labs[q]);
+            v.stride[q] = has(X.lab, labs[q]) ? X.l.stride[axis_of(X, labs[q])] : 0;
+        }
+        return v;
+    };
     int rc = RSTSR_OK;
-    if (nb * m * n == 0) {
+    if (nres == 0) {
         // nothing to write
     } else if (k == 0) {
-        rstsr_layout l = lc.to_abi();
+        rstsr_layout l = lres.to_abi();
         const double zero = 0.0;
         const float zf = 0.0f;
         const int64_t zi = 0;
         const void* z = t == RSTSR_F64 ? (const void*)&zero : t == RSTSR_F32 ? (const void*)&zf : (const void*)&zi;
         rc = rstsr_cuda_fill(ctx, cptr, &l, t, z);
     } else if (con.empty()) {
-        // outer product per batch: c[b, i, j] = a[b, i] * b[b, j] (broadcast multiply)
-        Layout va, vb;
-        const std::vector<int> ga[3] = {batch, fa, {}}, gb[3] = {batch, {}, fb};
-        rc = view3(ctx, t, A, ga, &va);
-        if (rc == RSTSR_OK) rc = view3(ctx, t, B, gb, &vb);
-        if (rc != RSTSR_OK) return fail_free(rc);
-        Layout xa = lc, xb = lc;
-        xa.offset = va.offset;
-        xa.stride[0] = va.stride[0];
-        xa.stride[1] = va.stride[1];
-        xa.stride[2] = 0;
-        xb.offset = vb.offset;
-        xb.stride[0] = vb.stride[0];
-        xb.stride[1] = 0;
-        xb.stride[2] = vb.stride[2];
-        if (nb == 1) xa.stride[0] = xb.stride[0] = 0;
-        rstsr_layout l0 = lc.to_abi(), l1 = xa.to_abi(), l2 = xb.to_abi();
+        // nothing contracted: the broadcast multiply over the result's axes
+        Layout xa = view_over(A, rlab), xb = view_over(B, rlab);
+        rstsr_layout l0 = lres.to_abi(), l1 = xa.to_abi(), l2 = xb.to_abi();
         rc = rstsr_cuda_binary(ctx, RSTSR_OP_MUL, t, cptr, &l0, A.ptr, &l1, B.ptr, &l2);
     } else {
-        Layout va, vb;
-        const std::vector<int> ga[3] = {batch, fa, con}, gb[3] = {batch, con, fb};
-        rc = view3(ctx, t, A, ga, &va);
-        if (rc == RSTSR_OK) rc = view3(ctx, t, B, gb, &vb);
-        if (rc != RSTSR_OK) return fail_free(rc);
-        rstsr_layout l0, l1, l2;
-        if (nb == 1) {  // a plain GEMM on the [M, K] x [K, N] views
-            Layout c2 = lc, a2 = va, b2 = vb;
-            c2.ndim = a2.ndim = b2.ndim = 2;
-            for (int q = 0; q < 2; ++q) {
-                c2.shape[q] = lc.shape[q + 1];
-                c2.stride[q] = lc.stride[q + 1];
-                a2.shape[q] = va.shape[q + 1];
-                a2.stride[q] = va.stride[q + 1];
-                b2.shape[q] = vb.shape[q + 1];
-                b2.stride[q] = vb.stride[q + 1];
-            }
-            l0 = c2.to_abi();
-            l1 = a2.to_abi();
-            l2 = b2.to_abi();
-        } else {
-            l0 = lc.to_abi();
-            l1 = va.to_abi();
-            l2 = vb.to_abi();
+        // [batch..., M, K] x [batch..., K, N] -> [batch..., M, N]
+        const int nbd = (int)bl.size();
+        Layout va = view_over(A, bl), vb = view_over(B, bl), vc;
+        vc.ndim = nbd + 2;
+        vc.offset = lres.offset;
+        for (int q = 0; q < nbd; ++q) {
+            vc.shape[q] = lres.shape[q];
+            vc.stride[q] = lres.stride[q];
         }
+        va.ndim = vb.ndim = nbd + 2;
+        int64_t e, st;
+        bool ok = true;
+        // M and N of C: merge its axes nbd.. (the M labels) and the rest (the N labels)
+        {
+            std::vector<int> axm, axn;
+            for (size_t q = 0; q < mlab.size(); ++q) axm.push_back(nbd + (int)q);
+            for (size_t q = 0; q < nlab.size(); ++q) axn.push_back(nbd + (int)mlab.size() + (int)q);
+            ok = merge_axes(lres, axm, &vc.shape[nbd], &vc.stride[nbd]) &&
+                 merge_axes(lres, axn, &vc.shape[nbd + 1], &vc.stride[nbd + 1]);
+        }
+        if (!ok) {
+            // the output's axes do not merge: compute into scratch instead
+            if (*wrote_out) {
+                *wrote_out = false;
+                std::vector<int64_t> shp;
+                for (int c : rlab) shp.push_back(ext.at(c));
+                lres = Layout::c_contig(shp.data(), (int)shp.size());
+                RSTSR_TRY(scratch_alloc(ctx, (size_t)std::max<int64_t>(nres, 1) * dtype_size(t), &owned));
+                cptr = owned;
+                for (int q = 0; q < nbd; ++q) vc.stride[q] = lres.stride[q];
+                vc.offset = 0;
+                std::vector<int> axm, axn;
+                for (size_t q = 0; q < mlab.size(); ++q) axm.push_back(nbd + (int)q);
+                for (size_t q = 0; q < nlab.size(); ++q) axn.push_back(nbd + (int)mlab.size() + (int)q);
+                merge_axes(lres, axm, &vc.shape[nbd], &vc.stride[nbd]);
+                merge_axes(lres, axn, &vc.shape[nbd + 1], &vc.stride[nbd + 1]);
+            } else {
+                return fail_free(fail(RSTSR_ERR_RUNTIME, "einsum: scratch result did not merge"));
+            }
+        }
+        // an empty M keeps C row-major for the grouped kernel (the stride of an extent-1 axis is free)
+        if (mlab.empty()) vc.stride[nbd] = vc.shape[nbd + 1] * std::max<int64_t>(vc.stride[nbd + 1], 1);
+        ok = merge_labels(A, mlab, &va.shape[nbd], &va.stride[nbd]) &&
+             merge_labels(A, klab, &va.shape[nbd + 1], &va.stride[nbd + 1]) &&
+             merge_labels(B, klab, &vb.shape[nbd], &vb.stride[nbd]) &&
+             merge_labels(B, nlab, &vb.shape[nbd + 1], &vb.stride[nbd + 1]);
+        if (!ok) return fail_free(fail(RSTSR_ERR_RUNTIME, "einsum: operand axes did not merge"));
+        (void)e;
+        (void)st;
+        rstsr_layout l0 = vc.to_abi(), l1 = va.to_abi(), l2 = vb.to_abi();
         rc = rstsr_cuda_matmul(ctx, t, cptr, &l0, A.ptr, &l1, B.ptr, &l2, 1.0, 0.0, RSTSR_ROW_MAJOR, opts);
     }
     if (rc != RSTSR_OK) return fail_free(rc);
     release(ctx, A);
     release(ctx, B);
     if (!*wrote_out) {
-        std::vector<int64_t> shp;
-        for (int c : rlab) shp.push_back(ext.at(c));
-        res->l = Layout::c_contig(shp.data(), (int)shp.size());
+        res->l = lres;
         res->ptr = cptr;
         res->owned = owned;
         res->lab = rlab;

@@ -188,10 +188,11 @@ __global__ void __launch_bounds__(256) spread_kernel(const SegPair segs, const u
 // MODE 0: Ozaki slices of each double x of a row with exponent e_r: y = x 2^-e_r
 //         as the fixed-point integer Y = y 2^63 (|Y| < 2^63; bits below 2^-63
 //         of the row maximum are dropped), then balanced base-128 digits from
-//         the top, d_s = round(Y / 2^(56 - 7s)) with Y reduced by each digit,
-//         so |d_0| <= 128 and |d_s| <= 64 after it. Slice s is d_s 2^(-7s),
-//         exact in bf16; a non-finite x puts itself in slice 0 and zeros after
-//         it. The column-0 threads also store the row exponents e_r.
+//         the top, the kept value being Y rounded to the nearest multiple of
+//         2^(56 - 7 (S-1)), ties up: |d_0| <= 128 and -64 <= d_s < 64 after it.
+//         Slice s is d_s 2^(-7s), exact in bf16; a non-finite x puts itself in
+//         slice 0 and zeros after it. The column-0 threads also store the row
+//         exponents e_r.
 // MODE 1: f32 three-term split hi / mid / lo.
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(lo)) |
@@ -254,19 +255,40 @@ __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitc
                 spv[v] = __uint_as_float(((uint32_t)(u >> 32) & 0x80000000u) | nan);
             }
         }
+        // Balanced base-128 digits without a per-digit rounding chain: with
+        // C = 64 (2^49 + 2^42 + ... + 2^(56 - 7 (S-1))) + 2^(55 - 7 (S-1)), the
+        // sum lo = (Y mod 2^56) + C (< 2^57) holds digit j + 64 (j >= 1) in bits
+        // [56 - 7j, 63 - 7j) and its carry out of bit 56 completes the top digit
+        // d_0 = (Y >> 56) + carry in [-128, 128]; the kept value is Y rounded to
+        // the nearest multiple of 2^(56 - 7 (S-1)), ties up, as a digit by digit
+        // round-half-up recurrence gives.
+        unsigned long long C = 1ull << (55 - 7 * (S - 1));
+        for (int sl = 1; sl < S; ++sl) C += 64ull << (56 - 7 * sl);
+        unsigned long long lo[8];
+        int top[8];
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const unsigned long long l = ((unsigned long long)Y[v] & ((1ull << 56) - 1)) + C;
+            top[v] = (int)(Y[v] >> 56) + (int)(l >> 56);
+            lo[v] = l;
+        }
         for (int sl = 0; sl < S; ++sl) {
             const int k = 56 - 7 * sl;
             const float scale = __int_as_float((127 - 7 * sl) << 23);
-            float d[8];
+            // 0x4B400000 | f is the float 12582912 + f (f < 2^22): (f - off) 2^(-7 sl) by
+            // one exact FFMA, no integer-to-float conversion
+            const float off = sl == 0 ? 12583040.0f : 12582976.0f;  // 12582912 + 128 / + 64
+            uint32_t bits[8];
 #pragma unroll
             for (int v = 0; v < 8; ++v) {
-                const long long dd = (Y[v] >> k) + ((Y[v] >> (k - 1)) & 1);  // round half up
-                Y[v] -= dd << k;
-                d[v] = __int2float_rn((int)dd) * scale;
-                if (sl == 0 && (special >> v) & 1u) d[v] = spv[v];
+                const uint32_t f = sl == 0 ? (uint32_t)(top[v] + 128) : (uint32_t)(lo[v] >> k) & 0x7Fu;
+                const float d = __fmaf_rn(__uint_as_float(0x4B400000u | f), scale, -off * scale);
+                bits[v] = __float_as_uint(d);
+                if (sl == 0 && (special >> v) & 1u) bits[v] = __float_as_uint(spv[v]);
             }
-            const uint4 w = make_uint4(pack_bf16(d[0], d[1]), pack_bf16(d[2], d[3]), pack_bf16(d[4], d[5]),
-                                       pack_bf16(d[6], d[7]));
+            // at most 8 significant bits: the bf16 is the float's upper half
+            const uint4 w = make_uint4(__byte_perm(bits[0], bits[1], 0x7632), __byte_perm(bits[2], bits[3], 0x7632),
+                                       __byte_perm(bits[4], bits[5], 0x7632), __byte_perm(bits[6], bits[7], 0x7632));
             if (oa) oa[sl * sa] = w;
             if (ob) ob[sl * sb] = w;
         }
