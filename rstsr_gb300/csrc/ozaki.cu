@@ -49,6 +49,7 @@ static thread_local int g_last_slices = 0;
 // rows start at `row0` of the item stack (slices, exponents, statistics).
 struct SegArg {
     int32_t n;
+    int32_t ublk;  // blocks of every item when all items of the side have one shape (else 0)
     SplitItem inl[2];
     const SplitItem* dev;
 };
@@ -67,6 +68,7 @@ __device__ __forceinline__ SplitItem seg_at(const SegArg& a, int i) { return a.n
 struct SegPair {
     SegArg a, b;
     int32_t rows_a;
+    int64_t a_blocks;  // flat blocks of the A items (the B items' blocks follow)
 };
 
 __device__ __forceinline__ int pair_blk0(const SegPair& sp, int i) {
@@ -75,12 +77,21 @@ __device__ __forceinline__ int pair_blk0(const SegPair& sp, int i) {
 }
 
 // The item of flat block `b` and the block's first row and column in it.
+// Items of one shape (a batch) find theirs by one division; mixed shapes by a
+// binary search over the items' first blocks.
 __device__ __forceinline__ SplitItem pair_block(const SegPair& sp, int64_t b, bool& is_b, int& r0, int& k0) {
-    int lo = 0, hi = sp.a.n + sp.b.n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (pair_blk0(sp, mid) <= b) lo = mid;
-        else hi = mid - 1;
+    int lo = 0;
+    if (b < sp.a_blocks && sp.a.ublk) {
+        lo = (int)(b / sp.a.ublk);
+    } else if (b >= sp.a_blocks && sp.b.ublk) {
+        lo = sp.a.n + (int)((b - sp.a_blocks) / sp.b.ublk);
+    } else {
+        int hi = sp.a.n + sp.b.n - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (pair_blk0(sp, mid) <= b) lo = mid;
+            else hi = mid - 1;
+        }
     }
     is_b = lo >= sp.a.n;
     const SplitItem it = is_b ? seg_at(sp.b, lo - sp.a.n) : seg_at(sp.a, lo);
@@ -103,8 +114,15 @@ __device__ __forceinline__ int exp_above(unsigned long long b) {
     return -1010 - __clzll((long long)b);  // subnormal: highest set bit p, m < 2^(p - 1073)
 }
 
+// Shared-tile column of element k of a row: each 8-element chunk j is rotated
+// by 2 (j / 2) so that the 8 threads reading chunks 0..7 of one row at the same
+// step hit 8 different 8-byte bank pairs (without the rotation, chunks 64
+// bytes apart collide 4 ways).
+__device__ __forceinline__ int tile_col(int k) { return (k & ~7) | ((k + 2 * ((k >> 4) & 3)) & 7); }
+
 // Load the block's 32 x 64 tile of an item into shared memory (zeros outside
-// the item), coalesced along whichever of rows / K is contiguous in memory.
+// the item), coalesced along whichever of rows / K is contiguous in memory;
+// element (r, k) lands at tile[r][tile_col(k)].
 template <typename T>
 __device__ __forceinline__ void load_tile(const SplitItem& it, int r0, int k0, T (*tile)[65]) {
     const T* X = (const T*)it.ptr;
@@ -115,7 +133,7 @@ __device__ __forceinline__ void load_tile(const SplitItem& it, int r0, int k0, T
         const int rr = kfast ? (t >> 6) + 4 * j : (t & 31);
         const int kk = kfast ? (t & 63) : (t >> 5) + 8 * j;
         const int r = r0 + rr, k = k0 + kk;
-        tile[rr][kk] = (r < it.R && k < it.K) ? X[(int64_t)r * it.s_row + (int64_t)k * it.s_k] : (T)0;
+        tile[rr][tile_col(kk)] = (r < it.R && k < it.K) ? X[(int64_t)r * it.s_row + (int64_t)k * it.s_k] : (T)0;
     }
 }
 
@@ -133,14 +151,31 @@ __global__ void __launch_bounds__(256) row_stats_kernel(const SegPair segs, unsi
     load_tile<T>(it, r0, k0, tile);
     __syncthreads();
     const int rr = threadIdx.x >> 3, kq = (threadIdx.x & 7) * 8;
-    unsigned long long mm = 0;
-    double ss = 0.0;
+    unsigned long long mm = 0, bv[8];
 #pragma unroll
     for (int v = 0; v < 8; ++v) {
-        const unsigned long long b =
-            (unsigned long long)__double_as_longlong((double)tile[rr][kq + v]) & 0x7FFFFFFFFFFFFFFFull;
-        mm = b > mm ? b : mm;
-        ss += __longlong_as_double((long long)b);
+        bv[v] = (unsigned long long)__double_as_longlong((double)tile[rr][tile_col(kq + v)]) & 0x7FFFFFFFFFFFFFFFull;
+        mm = bv[v] > mm ? bv[v] : mm;
+    }
+    // The sum of |x| only feeds the exponent-spread estimate: add the 8 values
+    // in FP32 on the scale of their largest binade (floats assembled from the
+    // doubles' bits; values below 2^-125 of it dropped) and rescale once, so
+    // that the FP64 pipe (a small fraction of GB300's FP32 rate) sees one
+    // multiply per 8 elements instead of 8 adds.
+    double ss = 0.0;
+    const int em = (int)(mm >> 52);
+    if (em > 0) {
+        float fs = 0.f;
+#pragma unroll
+        for (int v = 0; v < 8; ++v) {
+            const int e = (int)(bv[v] >> 52), d = e - em;
+            if (e > 0 && d > -126)
+                fs += __uint_as_float(((uint32_t)(127 + d) << 23) | (uint32_t)((bv[v] >> 29) & 0x7FFFFFu));
+        }
+        ss = (double)fs * __longlong_as_double((long long)((unsigned long long)em << 52));
+    } else {  // zeros and subnormals only
+#pragma unroll
+        for (int v = 0; v < 8; ++v) ss += __longlong_as_double((long long)bv[v]);
     }
 #pragma unroll
     for (int d = 4; d > 0; d >>= 1) {
@@ -239,7 +274,7 @@ __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitc
         float spv[8];            // its bf16-exact float (slice 0)
 #pragma unroll
         for (int v = 0; v < 8; ++v) {
-            const unsigned long long u = (unsigned long long)__double_as_longlong((double)tile[rr][kq + v]);
+            const unsigned long long u = (unsigned long long)__double_as_longlong((double)tile[rr][tile_col(kq + v)]);
             const int E = (int)((u >> 52) & 0x7FF);
             const long long mant =
                 (long long)(E ? (u & 0xFFFFFFFFFFFFFull) | (1ull << 52) : (u & 0xFFFFFFFFFFFFFull));
@@ -296,7 +331,7 @@ __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitc
         float h[8], m[8], l[8];
 #pragma unroll
         for (int v = 0; v < 8; ++v) {
-            const float x = (float)tile[rr][kq + v];
+            const float x = (float)tile[rr][tile_col(kq + v)];
             h[v] = __bfloat162float(__float2bfloat16_rn(x));
             const float r1 = x - h[v];
             m[v] = __bfloat162float(__float2bfloat16_rn(r1));
@@ -416,6 +451,22 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
     if ((s = make_segs(ctx, a_items, &segs.a, &dseg))) return cleanup(), s;
     if (dseg) owned.push_back(dseg);
     if ((s = make_segs(ctx, b_items, &segs.b, &dseg))) return cleanup(), s;
+    // one block count for every item of a side: the item of a block is a division
+    auto uniform_blocks = [](const std::vector<SplitItem>& v, int64_t* total) {
+        *total = 0;
+        int64_t first = -1;
+        bool same = true;
+        for (const SplitItem& it : v) {
+            const int64_t nb = (int64_t)((it.R + 31) / 32) * it.kblk;
+            *total += nb;
+            if (first < 0) first = nb;
+            same = same && nb == first;
+        }
+        return same && first > 0 && first <= INT32_MAX ? (int32_t)first : 0;
+    };
+    int64_t b_total = 0;
+    segs.a.ublk = uniform_blocks(a_items, &segs.a_blocks);
+    segs.b.ublk = uniform_blocks(b_items, &b_total);
     if (dseg) owned.push_back(dseg);
     // per-row statistics (Ozaki only); B rows follow A rows
     const size_t nst = (size_t)rows_a + rows_b;
