@@ -647,6 +647,66 @@ int tensordot_labels(int nda, int ndb, const int64_t* axes_a, const int64_t* axe
     return RSTSR_OK;
 }
 
+// Fused dot products: one warp per output element c[r] = sum_k a[r, k] b[r, k]
+// over a contracted axis contiguous in both operands (stride 1), four loads
+// of each operand in flight per lane, a shuffle reduction at the end. The
+// outputs' multi-indices (broadcast operands: stride 0) are decomposed from
+// the warp's row number.
+struct DotParams {
+    DevDims dims;  // the output's collapsed dims (inner first)
+    int64_t sc[RSTSR_MAX_NDIM], sa[RSTSR_MAX_NDIM], sb[RSTSR_MAX_NDIM];
+    int64_t oc, oa, ob;
+    int64_t K;
+    uint32_t rows;
+};
+
+template <typename T> struct DotAcc { using type = T; };
+template <> struct DotAcc<int32_t> { using type = uint32_t; };  // wrapping sums
+template <> struct DotAcc<int64_t> { using type = uint64_t; };
+
+template <typename T>
+__global__ void __launch_bounds__(256) vecdot_rows_kernel(T* __restrict__ c, const T* __restrict__ a,
+                                                          const T* __restrict__ b, const DotParams p) {
+    using A = typename DotAcc<T>::type;
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < p.rows; w += nw) {
+        int64_t oc = p.oc, oa = p.oa, ob = p.ob;
+        uint32_t rem = w;
+        for (int d = 0; d < p.dims.ndim; ++d) {
+            const uint32_t q = d + 1 < p.dims.ndim ? p.dims.div[d].div(rem) : 0;
+            const int64_t i = (int64_t)(rem - q * p.dims.shape[d]);
+            rem = q;
+            oc += i * p.sc[d];
+            oa += i * p.sa[d];
+            ob += i * p.sb[d];
+        }
+        const T* x = a + oa;
+        const T* y = b + ob;
+        A acc[4] = {A(0), A(0), A(0), A(0)};
+        for (int64_t k = lane; k < p.K; k += 128) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int64_t kk = k + 32 * u;
+                if (kk < p.K) acc[u] += (A)x[kk] * (A)y[kk];
+            }
+        }
+        A s = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) c[oc] = (T)s;
+    }
+}
+
+template <typename T>
+int launch_vecdot_rows(rstsr_ctx* ctx, const DotParams& p, void* c, const void* a, const void* b) {
+    const uint32_t cap = (uint32_t)ctx->num_sms * 64;  // warps
+    const uint32_t warps = p.rows < cap ? p.rows : cap;
+    vecdot_rows_kernel<T><<<(warps + 7) / 8, 256, 0, ctx->stream>>>(static_cast<T*>(c), static_cast<const T*>(a),
+                                                                      static_cast<const T*>(b), p);
+    return after_launch(ctx, "vecdot_rows_kernel");
+}
+
 }  // namespace
 
 }  // namespace rstsr
@@ -733,6 +793,39 @@ int rstsr_cuda_vecdot(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout
         return fail(RSTSR_ERR_INVALID_LAYOUT, "vecdot: a and b do not broadcast to c after the axis sum");
     RSTSR_TRY(check_write_layout(Cl, "vecdot"));
     if (Cl.size() == 0) return RSTSR_OK;
+    // fused path: the contracted axes merge into one axis of stride 1 in both
+    // operands, it is long enough for a warp, and the rows fit 32-bit indexing
+    {
+        std::vector<int> ax(as.ndim);
+        for (int d = 0; d < as.ndim; ++d) ax[d] = d;
+        int64_t ka, sa1, kb, sb1;
+        const bool fused_type = t == RSTSR_F64 || t == RSTSR_F32 || t == RSTSR_I32 || t == RSTSR_I64;
+        if (fused_type && merge_axes(as, ax, &ka, &sa1) && merge_axes(bs, ax, &kb, &sb1) && ka == kb &&
+            (sa1 == 1 || ka == 1) && (sb1 == 1 || kb == 1) && ka >= 32 && Cl.size() <= INT32_MAX) {
+            const Layout* ls[3] = {&Cl, &amb, &bmb};
+            IterSpace sp = make_iter_space(ls, 3);
+            DotParams p;
+            std::memset(&p, 0, sizeof(p));
+            p.dims = make_dev_dims(sp);
+            for (int d = 0; d < sp.ndim; ++d) {
+                p.sc[d] = sp.stride[0][d];
+                p.sa[d] = sp.stride[1][d];
+                p.sb[d] = sp.stride[2][d];
+            }
+            p.oc = sp.offset[0];
+            p.oa = sp.offset[1] + (as.offset - A.offset);
+            p.ob = sp.offset[2] + (bs.offset - B.offset);
+            p.K = ka;
+            p.rows = (uint32_t)Cl.size();
+            if (!a || !b || !c) return fail(RSTSR_ERR_INVALID_VALUE, "null data pointer");
+            switch (t) {
+                case RSTSR_F64: return launch_vecdot_rows<double>(ctx, p, c, a, b);
+                case RSTSR_F32: return launch_vecdot_rows<float>(ctx, p, c, a, b);
+                case RSTSR_I32: return launch_vecdot_rows<int32_t>(ctx, p, c, a, b);
+                default: return launch_vecdot_rows<int64_t>(ctx, p, c, a, b);
+            }
+        }
+    }
     // product over [c's axes..., contracted axes...] then the sum over the contracted axes
     Layout P, PA, PB;
     P.ndim = PA.ndim = PB.ndim = Cl.ndim + as.ndim;

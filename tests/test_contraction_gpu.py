@@ -248,3 +248,31 @@ def test_vecdot_axes_forms(cdev):
                                rtol=1e-13)
     with pytest.raises(RstsrError):
         rt.vecdot(a, rt.asarray(np.ones((6, 5, 3)), cdev))
+
+
+@pytest.mark.parametrize("sa,sb,order", [((300, 257), (300, 257), "C"), ((5, 1, 100), (3, 100), "C"),
+                                         ((64, 4096), (4096,), "C"), ((33, 40), (33, 40), "F")])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32, np.int64])
+def test_vecdot_fused_rows(cdev, sa, sb, order, dtype):
+    """Contracted axis contiguous in both operands (the one-warp-per-output
+    kernel), with broadcasting and a column-major device."""
+    dev = cdev
+    dev.set_default_order(order)
+    rng = np.random.default_rng(len(sa) + sa[-1])
+    xa = rng.standard_normal(sa).astype(dtype) if np.dtype(dtype).kind == "f" else \
+        rng.integers(-50, 50, sa).astype(dtype)
+    xb = rng.standard_normal(sb).astype(dtype) if np.dtype(dtype).kind == "f" else \
+        rng.integers(-50, 50, sb).astype(dtype)
+    if order == "C":
+        a, b = rt.asarray(xa, dev), rt.asarray(xb, dev)
+        got = rt.vecdot(a, b).to_numpy()
+        want = oracle_vecdot(xa, xb)
+    else:  # column-major: the first axis is contiguous; contract it
+        a = rt.from_host_layout(xa.ravel(order="F"), xa.shape, O.f_strides(xa.shape), 0, dev)
+        b = rt.from_host_layout(xb.ravel(order="F"), xb.shape, O.f_strides(xb.shape), 0, dev)
+        got = rt.vecdot(a, b, 0).to_numpy()
+        want = oracle_vecdot(np.ascontiguousarray(xa.T), np.ascontiguousarray(xb.T))
+    if np.dtype(dtype).kind == "f":
+        assert rel_err(got, want) <= (1e-13 if dtype == np.float64 else 1e-5)
+    else:
+        np.testing.assert_array_equal(got, want.astype(dtype))
