@@ -180,7 +180,15 @@ typedef enum {
     RSTSR_OP_SHR = 9,
     RSTSR_OP_MAXIMUM = 10,
     RSTSR_OP_MINIMUM = 11,
-    RSTSR_OP_POW = 12
+    RSTSR_OP_POW = 12,
+    /* op_ternary_common.rs:3-19 with the closures of
+     * feature_rayon/auto_impl/op_ternary_common.rs:6-80 (floats only unless noted) */
+    RSTSR_OP_ATAN2 = 13,        /* a.atan2(b) */
+    RSTSR_OP_COPYSIGN = 14,     /* Float::copysign(a, b) */
+    RSTSR_OP_HYPOT = 15,        /* a.hypot(b) */
+    RSTSR_OP_LOGADDEXP = 16,    /* (a.exp() + b.exp()).ln(), as the reference writes it */
+    RSTSR_OP_NEXTAFTER = 17,    /* nextafter(a, b) */
+    RSTSR_OP_FLOOR_DIVIDE = 18  /* floats: floor(a / b); integers: floor division (x / 0 = 0 here) */
 } rstsr_binary_op;
 
 /* Op*API::op_mutc_refa_refb (op_ternary_arithmetic.rs:3-48; CPU impl
@@ -222,13 +230,72 @@ typedef enum {
     RSTSR_UOP_SQUARE = 9,
     RSTSR_UOP_FLOOR = 10,
     RSTSR_UOP_CEIL = 11,
-    RSTSR_UOP_SIGN = 12,
-    RSTSR_UOP_RECIP = 13
+    RSTSR_UOP_SIGN = 12,        /* ExtNum::ext_sign: NaN -> NaN, +-0 -> 0, else +-1 */
+    RSTSR_UOP_RECIP = 13,
+    /* the rest of op_binary_common.rs:3-65 (auto_impl/op_binary_common.rs:10-40):
+     * float element types; CONJ, REAL and IMAG on every numeric type */
+    RSTSR_UOP_ACOS = 14,
+    RSTSR_UOP_ACOSH = 15,
+    RSTSR_UOP_ASIN = 16,
+    RSTSR_UOP_ASINH = 17,
+    RSTSR_UOP_ATAN = 18,
+    RSTSR_UOP_ATANH = 19,
+    RSTSR_UOP_COSH = 20,
+    RSTSR_UOP_EXPM1 = 21,
+    RSTSR_UOP_LOG1P = 22,
+    RSTSR_UOP_LOG2 = 23,
+    RSTSR_UOP_LOG10 = 24,
+    RSTSR_UOP_ROUND = 25,       /* half away from zero (Rust round) */
+    RSTSR_UOP_SINH = 26,
+    RSTSR_UOP_TAN = 27,
+    RSTSR_UOP_TRUNC = 28,
+    RSTSR_UOP_INV = 29,         /* recip */
+    RSTSR_UOP_CONJ = 30,        /* identity on real types */
+    RSTSR_UOP_REAL = 31,        /* identity on real types */
+    RSTSR_UOP_IMAG = 32         /* zero on real types */
 } rstsr_unary_op;
 
 /* c = op(a) (op_mutc_refa family); a in place when c == a with equal layouts. */
 int rstsr_cuda_unary(rstsr_ctx* ctx, rstsr_unary_op op, rstsr_dtype t,
                      void* c, const rstsr_layout* lc, const void* a, const rstsr_layout* la);
+
+/* Boolean-valued unary operators (auto_impl/op_binary_common.rs:94-120):
+ * IsFinite / IsInf / IsNan on float types; SignBit writes the reference's
+ * `is_positive()` (floats: sign bit clear, so +0, +inf and +NaN give true;
+ * signed integers: x > 0). c is BOOL. */
+typedef enum {
+    RSTSR_PRED_ISFINITE = 0,
+    RSTSR_PRED_ISINF = 1,
+    RSTSR_PRED_ISNAN = 2,
+    RSTSR_PRED_SIGNBIT = 3
+} rstsr_predicate_op;
+int rstsr_cuda_unary_predicate(rstsr_ctx* ctx, rstsr_predicate_op op, rstsr_dtype ta, void* c,
+                               const rstsr_layout* lc, const void* a, const rstsr_layout* la);
+
+/* Comparisons (OpEqualAPI ... OpLessEqualAPI, op_ternary_common.rs:3-19):
+ * c (BOOL) = a (op) b with PartialEq / PartialOrd (any comparison with NaN is
+ * false, != is true). la and lb are broadcast to lc. */
+typedef enum {
+    RSTSR_CMP_EQ = 0,
+    RSTSR_CMP_NE = 1,
+    RSTSR_CMP_GT = 2,
+    RSTSR_CMP_GE = 3,
+    RSTSR_CMP_LT = 4,
+    RSTSR_CMP_LE = 5
+} rstsr_compare_op;
+int rstsr_cuda_compare(rstsr_ctx* ctx, rstsr_compare_op op, rstsr_dtype t, void* c, const rstsr_layout* lc,
+                       const void* a, const rstsr_layout* la, const void* b, const rstsr_layout* lb);
+/* One operand a HOST scalar of type t (scalar_is_lhs as in rstsr_cuda_binary_scalar). */
+int rstsr_cuda_compare_scalar(rstsr_ctx* ctx, rstsr_compare_op op, rstsr_dtype t, void* c,
+                              const rstsr_layout* lc, const void* a, const rstsr_layout* la,
+                              const void* scalar, int32_t scalar_is_lhs);
+
+/* OpIsCloseAPI (op_ternary_common.rs:65-100; rstsr-dtype-traits/src/isclose.rs:92-105):
+ * c (BOOL) = |a - b| <= atol + rtol |b| (the difference in the operands' type,
+ * the test in f64) or (equal_nan and both NaN). */
+int rstsr_cuda_isclose(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc,
+                       const void* a, const rstsr_layout* la, const void* b, const rstsr_layout* lb,
+                       double rtol, double atol, int32_t equal_nan);
 
 /* Fused d = a * b + c (one pass). The reference evaluates `&a * &b + &c` as
  * OpMulAPI::op_mutc_refa_refb (tensor/operators/op_binary_arithmetic.rs:170-213)

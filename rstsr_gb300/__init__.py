@@ -23,6 +23,7 @@ from .tensor import (  # noqa: F401
     binary,
     binary_inplace,
     binary_scalar,
+    compare,
     bool_select,
     einsum,
     empty,
@@ -31,9 +32,11 @@ from .tensor import (  # noqa: F401
     from_host_layout,
     full,
     index_select,
+    isclose,
     matmul,
     matmul_into,
     pack_tri,
+    predicate,
     reduce_all,
     reduce_axes,
     reduce_axes_into,
@@ -45,5 +48,26 @@ from .tensor import (  # noqa: F401
     vecdot,
     zeros,
 )
+
+from . import _lib as _l
+
+
+def _install_op_functions():
+    """rt.isnan(a), rt.less(a, b), rt.atan2(a, b), rt.log1p(a), ... as module
+    functions named after rstsr's (the predicates, comparisons and the
+    element-wise math family)."""
+    g = globals()
+    for name in _l.PRED:
+        g[name] = (lambda n: lambda a: predicate(n, a))(name)
+    for name in _l.CMP:
+        g[name] = (lambda n: lambda a, b: compare(n, a, b))(name)
+    for name in ("atan2", "copysign", "hypot", "logaddexp", "nextafter", "floor_divide"):
+        g[name] = (lambda n: lambda a, b: binary(n, a, b) if isinstance(b, Tensor) else binary_scalar(n, a, b))(name)
+    for name in ("acos", "acosh", "asin", "asinh", "atan", "atanh", "cosh", "expm1", "log1p", "log2", "log10",
+                 "round", "sinh", "tan", "trunc", "inv", "conj", "real", "imag"):
+        g[name] = (lambda n: lambda a: unary(n, a))(name)
+
+
+_install_op_functions()
 
 __version__ = "0.1.0"

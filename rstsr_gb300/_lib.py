@@ -128,8 +128,13 @@ def np_dtype(code: int) -> np.dtype:
 
 
 # binary ops (rstsr_binary_op)
-OP = dict(add=0, sub=1, mul=2, div=3, rem=4, bitand=5, bitor=6, bitxor=7, shl=8, shr=9, maximum=10, minimum=11, pow=12)
-UOP = dict(neg=0, not_=1, abs=2, sqrt=3, exp=4, log=5, sin=6, cos=7, tanh=8, square=9, floor=10, ceil=11, sign=12, recip=13)
+OP = dict(add=0, sub=1, mul=2, div=3, rem=4, bitand=5, bitor=6, bitxor=7, shl=8, shr=9, maximum=10, minimum=11, pow=12,
+          atan2=13, copysign=14, hypot=15, logaddexp=16, nextafter=17, floor_divide=18)
+UOP = dict(neg=0, not_=1, abs=2, sqrt=3, exp=4, log=5, sin=6, cos=7, tanh=8, square=9, floor=10, ceil=11, sign=12, recip=13,
+           acos=14, acosh=15, asin=16, asinh=17, atan=18, atanh=19, cosh=20, expm1=21, log1p=22, log2=23, log10=24,
+           round=25, sinh=26, tan=27, trunc=28, inv=29, conj=30, real=31, imag=32)
+PRED = dict(isfinite=0, isinf=1, isnan=2, signbit=3)
+CMP = dict(equal=0, not_equal=1, greater=2, greater_equal=3, less=4, less_equal=5)
 RED = dict(sum=0, mean=1, var=2, std=3, min=4, max=5, prod=6, l2_norm=7, all=8, any=9, count_nonzero=10)
 
 _P = C.c_void_p
@@ -162,6 +167,10 @@ _SIGS = {
     "rstsr_cuda_binary_scalar": ([_P, _I, _I, _P, _L, _P, _L, _P, _I], C.c_int),
     "rstsr_cuda_binary_inplace": ([_P, _I, _I, _P, _L, _P, _L, _I], C.c_int),
     "rstsr_cuda_unary": ([_P, _I, _I, _P, _L, _P, _L], C.c_int),
+    "rstsr_cuda_unary_predicate": ([_P, _I, _I, _P, _L, _P, _L], C.c_int),
+    "rstsr_cuda_compare": ([_P, _I, _I, _P, _L, _P, _L, _P, _L], C.c_int),
+    "rstsr_cuda_compare_scalar": ([_P, _I, _I, _P, _L, _P, _L, _P, _I], C.c_int),
+    "rstsr_cuda_isclose": ([_P, _I, _P, _L, _P, _L, _P, _L, C.c_double, C.c_double, _I], C.c_int),
     "rstsr_cuda_fma": ([_P, _I, _P, _L, _P, _L, _P, _L, _P, _L], C.c_int),
     "rstsr_cuda_reduce_out_dtype": ([_I, _I, C.POINTER(C.c_int)], C.c_int),
     "rstsr_cuda_reduce_all": ([_P, _I, _I, _P, _L, _P], C.c_int),

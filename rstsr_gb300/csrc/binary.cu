@@ -16,9 +16,57 @@ namespace rstsr {
 template <typename T>
 using UnsignedOf = typename std::make_unsigned<T>::type;
 
+// nextafter on the bit pattern of a 16-bit float (half or bfloat16): the
+// neighbour of x toward y, y itself when equal, the smallest subnormal of y's
+// sign from a zero, NaN when either is NaN.
+template <typename T>
+__device__ __forceinline__ uint16_t bits16(T v) {
+    if constexpr (std::is_same<T, __half>::value) return __half_as_ushort(v);
+    else return __bfloat16_as_ushort(v);
+}
+template <typename T>
+__device__ __forceinline__ T from_bits16(uint16_t u) {
+    if constexpr (std::is_same<T, __half>::value) return __ushort_as_half(u);
+    else return __ushort_as_bfloat16(u);
+}
+template <typename T>
+__device__ __forceinline__ T nextafter_t(T a, T b) {
+    if constexpr (std::is_same<T, double>::value) {
+        return nextafter(a, b);
+    } else if constexpr (std::is_same<T, float>::value) {
+        return nextafterf(a, b);
+    } else {
+        const float x = widen(a), y = widen(b);
+        if (x != x || y != y) return narrow<T>(x + y);
+        uint16_t ux = bits16(a);
+        const uint16_t uy = bits16(b);
+        if (ux == uy) return b;
+        const uint16_t ax = ux & 0x7FFF, ay = uy & 0x7FFF;
+        if (ax == 0) {
+            if (ay == 0) return b;
+            ux = (uint16_t)((uy & 0x8000) | 1);
+        } else if (ax > ay || ((ux ^ uy) & 0x8000)) {
+            ux = (uint16_t)(ux - 1);
+        } else {
+            ux = (uint16_t)(ux + 1);
+        }
+        return from_bits16<T>(ux);
+    }
+}
+
 template <typename T, int OP, bool IS_BOOL>
 __device__ __forceinline__ T binop(T a, T b) {
-    if constexpr (is_float_v<T>) {
+    if constexpr (is_float_v<T> && OP == RSTSR_OP_NEXTAFTER) {
+        return nextafter_t<T>(a, b);
+    } else if constexpr (is_float_v<T> && OP == RSTSR_OP_FLOOR_DIVIDE) {
+        // Float::floor(a / b): the quotient rounded to T first (matters for 16-bit types)
+        return narrow<T>(floor(widen(narrow<T>(widen(a) / widen(b)))));
+    } else if constexpr (is_float_v<T> && OP == RSTSR_OP_LOGADDEXP) {
+        // (a.exp() + b.exp()).ln(), each step rounded to T as the reference evaluates it
+        using C = typename Compute<T>::type;
+        const C ea = widen(narrow<T>(exp(widen(a)))), eb = widen(narrow<T>(exp(widen(b))));
+        return narrow<T>(log(widen(narrow<T>(ea + eb))));
+    } else if constexpr (is_float_v<T>) {
         using C = typename Compute<T>::type;
         C x = widen(a), y = widen(b);
         C r;
@@ -30,6 +78,9 @@ __device__ __forceinline__ T binop(T a, T b) {
         else if constexpr (OP == RSTSR_OP_MAXIMUM) r = fmax(x, y);
         else if constexpr (OP == RSTSR_OP_MINIMUM) r = fmin(x, y);
         else if constexpr (OP == RSTSR_OP_POW) r = pow(x, y);
+        else if constexpr (OP == RSTSR_OP_ATAN2) r = atan2(x, y);
+        else if constexpr (OP == RSTSR_OP_COPYSIGN) r = copysign(x, y);
+        else if constexpr (OP == RSTSR_OP_HYPOT) r = hypot(x, y);
         else r = x;
         return narrow<T>(r);
     } else if constexpr (IS_BOOL) {
@@ -59,7 +110,17 @@ __device__ __forceinline__ T binop(T a, T b) {
         else if constexpr (OP == RSTSR_OP_SHR) return (T)(a >> ((U)b & (bits - 1)));
         else if constexpr (OP == RSTSR_OP_MAXIMUM) return a > b ? a : b;
         else if constexpr (OP == RSTSR_OP_MINIMUM) return a < b ? a : b;
-        else {  // POW: wrapping power, exponent taken as unsigned
+        else if constexpr (OP == RSTSR_OP_FLOOR_DIVIDE) {
+            // Integer::div_floor; x / 0 = 0 here (the reference panics); MIN / -1 wraps
+            if (b == 0) return (T)0;
+            if constexpr (std::is_signed<T>::value) {
+                if (b == (T)-1) return (T)((U)0 - (U)a);
+                const T q = (T)(a / b), r = (T)(a % b);
+                return (r != 0 && ((r < 0) != (b < 0))) ? (T)(q - 1) : q;
+            } else {
+                return (T)(a / b);
+            }
+        } else {  // POW: wrapping power, exponent taken as unsigned
             U base = (U)a, e = (U)b, r = 1;
             while (e) {
                 if (e & 1) r = (U)(r * base);
@@ -99,14 +160,17 @@ struct FmaF {
 static bool op_valid(int op, rstsr_dtype t) {
     const bool bitop = op == RSTSR_OP_BITAND || op == RSTSR_OP_BITOR || op == RSTSR_OP_BITXOR ||
                        op == RSTSR_OP_SHL || op == RSTSR_OP_SHR;
+    const bool float_only = op == RSTSR_OP_ATAN2 || op == RSTSR_OP_COPYSIGN || op == RSTSR_OP_HYPOT ||
+                            op == RSTSR_OP_LOGADDEXP || op == RSTSR_OP_NEXTAFTER;
     if (is_float_dtype(t)) return !bitop;
     if (t == RSTSR_BOOL) return op == RSTSR_OP_BITAND || op == RSTSR_OP_BITOR || op == RSTSR_OP_BITXOR;
-    return true;
+    return !float_only;
 }
 
 static int check_op_dtype(int op, rstsr_dtype t) {
     if (!dtype_valid(t)) return fail(RSTSR_ERR_INVALID_VALUE, "unknown dtype");
-    if (op < RSTSR_OP_ADD || op > RSTSR_OP_POW) return fail(RSTSR_ERR_INVALID_VALUE, "unknown binary operator");
+    if (op < RSTSR_OP_ADD || op > RSTSR_OP_FLOOR_DIVIDE)
+        return fail(RSTSR_ERR_INVALID_VALUE, "unknown binary operator");
     if (!op_valid(op, t))
         return fail(RSTSR_ERR_INVALID_VALUE,
                     std::string("operator ") + std::to_string(op) + " is not defined on " + dtype_name(t));
@@ -134,7 +198,18 @@ __device__ __forceinline__ T binop_rt(int op, T a, T b) {
             case RSTSR_OP_MAXIMUM: return binop<T, RSTSR_OP_MAXIMUM, false>(a, b);
             case RSTSR_OP_MINIMUM: return binop<T, RSTSR_OP_MINIMUM, false>(a, b);
             case RSTSR_OP_POW: return binop<T, RSTSR_OP_POW, false>(a, b);
+            case RSTSR_OP_FLOOR_DIVIDE: return binop<T, RSTSR_OP_FLOOR_DIVIDE, false>(a, b);
             default: break;
+        }
+        if constexpr (is_float_v<T>) {
+            switch (op) {
+                case RSTSR_OP_ATAN2: return binop<T, RSTSR_OP_ATAN2, false>(a, b);
+                case RSTSR_OP_COPYSIGN: return binop<T, RSTSR_OP_COPYSIGN, false>(a, b);
+                case RSTSR_OP_HYPOT: return binop<T, RSTSR_OP_HYPOT, false>(a, b);
+                case RSTSR_OP_LOGADDEXP: return binop<T, RSTSR_OP_LOGADDEXP, false>(a, b);
+                case RSTSR_OP_NEXTAFTER: return binop<T, RSTSR_OP_NEXTAFTER, false>(a, b);
+                default: break;
+            }
         }
         if constexpr (!is_float_v<T>) {
             switch (op) {

@@ -33,7 +33,7 @@ static bool uop_valid(int op, rstsr_dtype t) {
     if (t == RSTSR_BOOL) return op == RSTSR_UOP_NOT;
     if (is_float_dtype(t)) return op != RSTSR_UOP_NOT;
     return op == RSTSR_UOP_NEG || op == RSTSR_UOP_NOT || op == RSTSR_UOP_ABS || op == RSTSR_UOP_SQUARE ||
-           op == RSTSR_UOP_SIGN;
+           op == RSTSR_UOP_SIGN || op == RSTSR_UOP_CONJ || op == RSTSR_UOP_REAL || op == RSTSR_UOP_IMAG;
 }
 
 // Floating-point unary math in the compute type (float or double), kept out
@@ -52,8 +52,27 @@ __device__ __noinline__ C float_unary(int op, C x) {
         case RSTSR_UOP_SQUARE: return x * x;
         case RSTSR_UOP_FLOOR: return floor(x);
         case RSTSR_UOP_CEIL: return ceil(x);
-        case RSTSR_UOP_SIGN: return (x != x) ? x : copysign((C)1, x);  // Rust signum
-        default: return (C)1 / x;                                      // RECIP
+        // ExtNum::ext_sign (rstsr-dtype-traits/src/ext_num.rs:166-178): NaN stays, zeros give 0
+        case RSTSR_UOP_SIGN: return (x != x) ? x : (x > (C)0 ? (C)1 : (x < (C)0 ? (C)-1 : (C)0));
+        case RSTSR_UOP_ACOS: return acos(x);
+        case RSTSR_UOP_ACOSH: return acosh(x);
+        case RSTSR_UOP_ASIN: return asin(x);
+        case RSTSR_UOP_ASINH: return asinh(x);
+        case RSTSR_UOP_ATAN: return atan(x);
+        case RSTSR_UOP_ATANH: return atanh(x);
+        case RSTSR_UOP_COSH: return cosh(x);
+        case RSTSR_UOP_EXPM1: return expm1(x);
+        case RSTSR_UOP_LOG1P: return log1p(x);
+        case RSTSR_UOP_LOG2: return log2(x);
+        case RSTSR_UOP_LOG10: return log10(x);
+        case RSTSR_UOP_ROUND: return round(x);  // half away from zero, as Rust's round
+        case RSTSR_UOP_SINH: return sinh(x);
+        case RSTSR_UOP_TAN: return tan(x);
+        case RSTSR_UOP_TRUNC: return trunc(x);
+        case RSTSR_UOP_CONJ:
+        case RSTSR_UOP_REAL: return x;
+        case RSTSR_UOP_IMAG: return (C)0;
+        default: return (C)1 / x;  // RECIP, INV
     }
 }
 
@@ -72,6 +91,9 @@ struct UnRtF {
                 case RSTSR_UOP_NOT: return unop<T, RSTSR_UOP_NOT, false>(a);
                 case RSTSR_UOP_ABS: return unop<T, RSTSR_UOP_ABS, false>(a);
                 case RSTSR_UOP_SQUARE: return unop<T, RSTSR_UOP_SQUARE, false>(a);
+                case RSTSR_UOP_CONJ:
+                case RSTSR_UOP_REAL: return a;
+                case RSTSR_UOP_IMAG: return (T)0;
                 default: return unop<T, RSTSR_UOP_SIGN, false>(a);
             }
         }
@@ -96,7 +118,7 @@ extern "C" int rstsr_cuda_unary(rstsr_ctx* ctx, rstsr_unary_op op, rstsr_dtype t
     RSTSR_TRY(check_layout(lc, "c"));
     RSTSR_TRY(check_layout(la, "a"));
     if (!dtype_valid(t)) return fail(RSTSR_ERR_INVALID_VALUE, "unknown dtype");
-    if (op < RSTSR_UOP_NEG || op > RSTSR_UOP_RECIP) return fail(RSTSR_ERR_INVALID_VALUE, "unknown unary operator");
+    if (op < RSTSR_UOP_NEG || op > RSTSR_UOP_IMAG) return fail(RSTSR_ERR_INVALID_VALUE, "unknown unary operator");
     if (!uop_valid(op, t))
         return fail(RSTSR_ERR_INVALID_VALUE,
                     std::string("unary operator ") + std::to_string(op) + " is not defined on " + dtype_name(t));

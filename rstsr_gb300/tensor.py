@@ -1030,3 +1030,69 @@ def vecdot(a: Tensor, b: Tensor, axes=None) -> Tensor:
     call("rstsr_cuda_vecdot", a.device.ctx, a.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
          C.c_void_p(a.ptr), C.byref(a.layout()), C.c_void_p(b.ptr), C.byref(b.layout()), ka, kb, len(xa), order)
     return out
+
+
+# ----------------------------------------- predicates, comparisons, isclose
+
+
+def _bool_out_like(lc: Layout, device: DeviceCuda) -> Tensor:
+    _, hi = _bounds(lc.shape_t, lc.stride_t, lc.offset)
+    return Tensor(Storage(device, max(hi, 1)), lc.shape_t, lc.stride_t, 0, _lib.BOOL)
+
+
+def predicate(op: str, a: Tensor) -> Tensor:
+    """isfinite / isinf / isnan / signbit (bool output, a's K-order layout).
+    signbit is the reference's `is_positive()`: true for +0, +inf, +NaN."""
+    lk = Layout()
+    call("rstsr_cuda_layout_for_array_copy", C.byref(a.layout()), b"K", C.byref(lk))
+    out = _bool_out_like(lk, a.device)
+    call("rstsr_cuda_unary_predicate", a.device.ctx, _lib.PRED[op], a.dtype_code, C.c_void_p(out.ptr),
+         C.byref(out.layout()), C.c_void_p(a.ptr), C.byref(a.layout()))
+    return out
+
+
+def compare(op: str, a, b) -> Tensor:
+    """equal / not_equal / greater / greater_equal / less / less_equal with
+    broadcasting (bool output); either side may be a Python scalar."""
+    if not isinstance(a, Tensor):
+        return _compare_scalar(op, b, a, True)
+    if not isinstance(b, Tensor):
+        return _compare_scalar(op, a, b, False)
+    _same_device(a, b)
+    if a.dtype_code != b.dtype_code:
+        raise RstsrError(2, f"dtype mismatch {a.dtype} vs {b.dtype}")
+    order = a.device.default_order
+    la, lb = broadcast_layouts(a, b, order)
+    lc = Layout()
+    call("rstsr_cuda_layout_binary_op", C.byref(la), C.byref(lb), order, C.byref(lc))
+    out = _bool_out_like(lc, a.device)
+    call("rstsr_cuda_compare", a.device.ctx, _lib.CMP[op], a.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
+         C.c_void_p(a.ptr), C.byref(la), C.c_void_p(b.ptr), C.byref(lb))
+    return out
+
+
+def _compare_scalar(op: str, t: Tensor, value, scalar_is_lhs: bool) -> Tensor:
+    lk = Layout()
+    call("rstsr_cuda_layout_for_array_copy", C.byref(t.layout()), b"K", C.byref(lk))
+    out = _bool_out_like(lk, t.device)
+    s = _scalar_bytes(value, t.dtype_code)
+    call("rstsr_cuda_compare_scalar", t.device.ctx, _lib.CMP[op], t.dtype_code, C.c_void_p(out.ptr),
+         C.byref(out.layout()), C.c_void_p(t.ptr), C.byref(t.layout()), s, 1 if scalar_is_lhs else 0)
+    return out
+
+
+def isclose(a: Tensor, b: Tensor, rtol: float = 1.0e-5, atol: float = 1.0e-8, equal_nan: bool = False) -> Tensor:
+    """isclose (rstsr-dtype-traits/src/isclose.rs:92-105): |a - b| <= atol +
+    rtol |b| (not symmetric), or both NaN with equal_nan; bool output."""
+    _same_device(a, b)
+    if a.dtype_code != b.dtype_code:
+        raise RstsrError(2, f"dtype mismatch {a.dtype} vs {b.dtype}")
+    order = a.device.default_order
+    la, lb = broadcast_layouts(a, b, order)
+    lc = Layout()
+    call("rstsr_cuda_layout_binary_op", C.byref(la), C.byref(lb), order, C.byref(lc))
+    out = _bool_out_like(lc, a.device)
+    call("rstsr_cuda_isclose", a.device.ctx, a.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()),
+         C.c_void_p(a.ptr), C.byref(la), C.c_void_p(b.ptr), C.byref(lb), float(rtol), float(atol),
+         1 if equal_nan else 0)
+    return out
