@@ -395,6 +395,7 @@ def run_gpu(args):
             result["small_f64"] = run_small_section(dev, stream)
             result["tri_index"] = run_tri_index_section(dev, stream)
             result["contraction"] = run_contraction_section(dev, stream)
+            result["contraction"].update(run_blas3_section(dev, stream))
         if not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline(args)
     if world > 1:
@@ -865,6 +866,71 @@ def run_contraction_section(dev, stream, P=1000, nao=350, nocc=50, nvir=300, vec
     return out
 
 
+def run_blas3_section(dev, stream, n_syrk=8192, k_syrk=2048, n=4096):
+    """SYRK (n_syrk x k_syrk, lower, beta 0.5), TRSM (n x n lower, n right-hand
+    sides) and SYMM (n x n x n) in f64 through the split GEMM, against torch's
+    FP64 cuBLAS calls on the same data (A A^T, solve_triangular, matmul); TFLOP/s
+    with the conventional counts (SYRK n(n+1)k, TRSM n^2 m, SYMM 2 n^2 m) and
+    the relative Frobenius error against the FP64 result."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    out = {}
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((n_syrk, k_syrk))
+    c = rng.standard_normal((n_syrk, n_syrk))
+    ta, tc = rt.asarray(a, dev), rt.asarray(c, dev)
+    ga = torch.from_numpy(a).cuda()
+    rt.syrk(ta, tc, "L", "N", 1.0, 0.5)
+    sec = _time_events(stream, lambda: rt.syrk(ta, tc, "L", "N", 1.0, 0.0), 3)
+    sec_t = _time_events(stream, lambda: ga @ ga.T, 1)
+    w = rt.empty((n_syrk, n_syrk), np.float64, dev)
+    rt.syrk(ta, w, "L", "N", 1.0, 0.0)
+    ref = torch.tril(ga @ ga.T)
+    err = (torch.linalg.norm(torch.tril(torch.as_tensor(w.to_numpy()).cuda()) - ref) / torch.linalg.norm(ref)).item()
+    fl = float(n_syrk) * (n_syrk + 1) * k_syrk
+    out["syrk_f64"] = {"n": n_syrk, "k": k_syrk, "tflops": round(fl / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
+                       "torch_fp64_tflops": round(fl / sec_t / 1e12, 3), "rel_err_frobenius": err}
+    del ta, tc, ga, w, ref
+    torch.cuda.empty_cache()
+    L = np.tril(rng.standard_normal((n, n)) * 0.02) + np.eye(n) * 2.0
+    B = rng.standard_normal((n, n))
+    tL, tB = rt.asarray(L, dev), rt.asarray(B, dev)
+    gL, gB = torch.from_numpy(L).cuda(), torch.from_numpy(B).cuda()
+    work = rt.empty((n, n), np.float64, dev)
+
+    def solve():
+        rt.assign(work, tB)
+        rt.trsm(tL, work, "L", "L", "N", "N")
+
+    solve()
+    sec = _time_events(stream, solve, 3)
+    sec_t = _time_events(stream, lambda: torch.linalg.solve_triangular(gL, gB, upper=False), 1)
+    ref = torch.linalg.solve_triangular(gL, gB, upper=False)
+    err = (torch.linalg.norm(torch.as_tensor(work.to_numpy()).cuda() - ref) / torch.linalg.norm(ref)).item()
+    fl = float(n) * n * n
+    out["trsm_f64"] = {"m": n, "n": n, "tflops": round(fl / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
+                       "torch_fp64_tflops": round(fl / sec_t / 1e12, 3), "rel_err_frobenius": err,
+                       "note": "includes the copy of B into the work matrix"}
+    S = rng.standard_normal((n, n))
+    S = (S + S.T) / 2
+    tS = rt.asarray(S, dev)
+    tC = rt.empty((n, n), np.float64, dev)
+    gS = torch.from_numpy(S).cuda()
+    rt.symm(tS, tB, tC, "L", "L")
+    sec = _time_events(stream, lambda: rt.symm(tS, tB, tC, "L", "L"), 3)
+    sec_t = _time_events(stream, lambda: gS @ gB, 1)
+    ref = gS @ gB
+    err = (torch.linalg.norm(torch.as_tensor(tC.to_numpy()).cuda() - ref) / torch.linalg.norm(ref)).item()
+    fl = 2.0 * n * n * n
+    out["symm_f64"] = {"m": n, "n": n, "tflops": round(fl / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
+                       "torch_fp64_tflops": round(fl / sec_t / 1e12, 3), "rel_err_frobenius": err}
+    del tL, tB, gL, gB, work, tS, tC, gS, ref
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_contraction_only(args):
     """Only the contraction section (profiling)."""
     import torch
@@ -875,7 +941,9 @@ def run_contraction_only(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     dev.set_stream(stream.cuda_stream)
-    return {"section": "contraction", "results": run_contraction_section(dev, stream, P=args.ein_p)}
+    res = run_contraction_section(dev, stream, P=args.ein_p)
+    res.update(run_blas3_section(dev, stream))
+    return {"section": "contraction", "results": res}
 
 
 def run_tri_index_only(args):

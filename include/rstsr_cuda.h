@@ -532,6 +532,31 @@ int rstsr_cuda_vecdot(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout
                       const void* a, const rstsr_layout* la, const void* b, const rstsr_layout* lb,
                       const int64_t* axes_a, const int64_t* axes_b, int32_t naxes, rstsr_order order);
 
+/* BLAS-3 drivers beyond GEMM (CBLAS conventions; F64 or F32; alpha / beta as
+ * doubles; opts as for rstsr_cuda_gemm). */
+
+/* SYRK (DeviceSYRKAPI::syrk, rstsr-core/src/operators/matmul.rs:64-78): the
+ * uplo ('L' | 'U') triangle of C (n x n) = alpha op(A) op(A)^T + beta C, op(A)
+ * = A (trans 'N', A n x k) or A^T ('T', A k x n); the other triangle of C is not
+ * touched, and C is not read when beta = 0. */
+int rstsr_cuda_syrk(rstsr_ctx* ctx, rstsr_order order, char uplo, char trans, int64_t n, int64_t k,
+                    double alpha, const void* a, int64_t lda, double beta, void* c, int64_t ldc,
+                    rstsr_dtype t, const rstsr_gemm_opts* opts);
+
+/* SYMM (driver_syhemm, rstsr-blas-traits/src/blas3/syhemm.rs:5-19): C (m x n) =
+ * alpha A B + beta C (side 'L', A m x m) or alpha B A + beta C ('R', A n x n),
+ * A symmetric and read from its uplo triangle only. */
+int rstsr_cuda_symm(rstsr_ctx* ctx, rstsr_order order, char side, char uplo, int64_t m, int64_t n,
+                    double alpha, const void* a, int64_t lda, const void* b, int64_t ldb, double beta,
+                    void* c, int64_t ldc, rstsr_dtype t, const rstsr_gemm_opts* opts);
+
+/* TRSM (driver_trsm, rstsr-blas-traits/src/blas3/trsm.rs:5-18): B (m x n) :=
+ * alpha op(A)^-1 B (side 'L', A m x m) or alpha B op(A)^-1 ('R', A n x n), A
+ * triangular in its uplo triangle, diag 'U' (unit, not read) or 'N'. */
+int rstsr_cuda_trsm(rstsr_ctx* ctx, rstsr_order order, char side, char uplo, char transa, char diag,
+                    int64_t m, int64_t n, double alpha, const void* a, int64_t lda, void* b, int64_t ldb,
+                    rstsr_dtype t, const rstsr_gemm_opts* opts);
+
 /* ---------------------------------------------------------------- graphs */
 
 /* Capture every call made on the context between begin and end into a CUDA

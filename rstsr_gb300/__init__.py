@@ -40,8 +40,11 @@ from .tensor import (  # noqa: F401
     reduce_all,
     reduce_axes,
     reduce_axes_into,
+    symm,
+    syrk,
     take,
     tensordot,
+    trsm,
     to_contig,
     unary,
     unpack_tri,

@@ -204,6 +204,21 @@ _SIGS = {
     ),
     "rstsr_cuda_matmul": ([_P, _I, _P, _L, _P, _L, _P, _L, C.c_double, C.c_double, _I, C.POINTER(GemmOpts)], C.c_int),
     "rstsr_cuda_matmul_layout": ([_L, _L, _I, _L], C.c_int),
+    "rstsr_cuda_syrk": (
+        [_P, _I, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_double, _P, C.c_int64, C.c_double, _P, C.c_int64,
+         _I, C.POINTER(GemmOpts)],
+        C.c_int,
+    ),
+    "rstsr_cuda_symm": (
+        [_P, _I, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_double, _P, C.c_int64, _P, C.c_int64, C.c_double,
+         _P, C.c_int64, _I, C.POINTER(GemmOpts)],
+        C.c_int,
+    ),
+    "rstsr_cuda_trsm": (
+        [_P, _I, C.c_char, C.c_char, C.c_char, C.c_char, C.c_int64, C.c_int64, C.c_double, _P, C.c_int64, _P,
+         C.c_int64, _I, C.POINTER(GemmOpts)],
+        C.c_int,
+    ),
     "rstsr_cuda_gemm_grouped": ([_P, _I, C.POINTER(GemmProblem), _I, C.POINTER(GemmOpts)], C.c_int),
     "rstsr_cuda_last_ozaki_slices": ([], C.c_int32),
     "rstsr_cuda_graph_begin": ([_P], C.c_int),

@@ -1096,3 +1096,65 @@ def isclose(a: Tensor, b: Tensor, rtol: float = 1.0e-5, atol: float = 1.0e-8, eq
          C.c_void_p(a.ptr), C.byref(la), C.c_void_p(b.ptr), C.byref(lb), float(rtol), float(atol),
          1 if equal_nan else 0)
     return out
+
+
+# ---------------------------------------------------------- BLAS-3 drivers
+
+
+def _blas_operand(t: Tensor):
+    """(order, leading dimension) of a 2-D tensor with a unit stride."""
+    if t.ndim != 2:
+        raise RstsrError(1, "a BLAS operand is a 2-D tensor")
+    r, c = t.shape
+    if t.stride[1] == 1 and t.stride[0] >= max(c, 1):
+        return ROW_MAJOR, t.stride[0]
+    if t.stride[0] == 1 and t.stride[1] >= max(r, 1):
+        return COL_MAJOR, t.stride[1]
+    if r <= 1 or c <= 1:
+        return ROW_MAJOR, max(c, 1)
+    raise RstsrError(1, "a BLAS operand needs a unit stride along one axis")
+
+
+def _same_order(*ts: Tensor):
+    orders = {_blas_operand(t)[0] for t in ts}
+    if len(orders) != 1:
+        raise RstsrError(1, "BLAS operands must share one memory order")
+    return orders.pop()
+
+
+def _ptr(t: Tensor) -> C.c_void_p:
+    return C.c_void_p(t.ptr + t.offset * t.itemsize)
+
+
+def syrk(a: Tensor, c: Tensor, uplo="L", trans="N", alpha: float = 1.0, beta: float = 0.0,
+         precision: int = 0, slices: int = 0) -> Tensor:
+    """c's uplo triangle = alpha op(a) op(a)^T + beta c (the other triangle kept)."""
+    order = _same_order(a, c)
+    n = c.shape[0]
+    k = a.shape[1] if trans in ("N", "n") else a.shape[0]
+    call("rstsr_cuda_syrk", a.device.ctx, order, uplo.encode(), trans.encode(), n, k, float(alpha), _ptr(a),
+         _blas_operand(a)[1], float(beta), _ptr(c), _blas_operand(c)[1], a.dtype_code,
+         C.byref(_gemm_opts(precision, slices)))
+    return c
+
+
+def symm(a: Tensor, b: Tensor, c: Tensor, side="L", uplo="L", alpha: float = 1.0, beta: float = 0.0,
+         precision: int = 0, slices: int = 0) -> Tensor:
+    """c = alpha a b + beta c (side L) or alpha b a + beta c (side R), a read from its uplo triangle."""
+    order = _same_order(a, b, c)
+    m, n = c.shape
+    call("rstsr_cuda_symm", a.device.ctx, order, side.encode(), uplo.encode(), m, n, float(alpha), _ptr(a),
+         _blas_operand(a)[1], _ptr(b), _blas_operand(b)[1], float(beta), _ptr(c), _blas_operand(c)[1], a.dtype_code,
+         C.byref(_gemm_opts(precision, slices)))
+    return c
+
+
+def trsm(a: Tensor, b: Tensor, side="L", uplo="L", transa="N", diag="N", alpha: float = 1.0,
+         precision: int = 0, slices: int = 0) -> Tensor:
+    """b := alpha op(a)^-1 b (side L) or alpha b op(a)^-1 (side R), in place."""
+    order = _same_order(a, b)
+    m, n = b.shape
+    call("rstsr_cuda_trsm", a.device.ctx, order, side.encode(), uplo.encode(), transa.encode(), diag.encode(), m, n,
+         float(alpha), _ptr(a), _blas_operand(a)[1], _ptr(b), _blas_operand(b)[1], a.dtype_code,
+         C.byref(_gemm_opts(precision, slices)))
+    return b
