@@ -13,9 +13,9 @@
 // indexed axis is innermost, stores stay coalesced and loads gather.
 //
 // The index list arrives in HOST memory (the reference's `&[usize]`). Up to
-// kIdxInline indices ride in the kernel parameters (no copy, valid inside a
-// graph capture: the list is baked into the captured launch); longer lists
-// are copied to stream-ordered scratch first.
+// kIdxInline indices (as int32, extents below 2^31) ride in the kernel
+// parameters (no copy, valid inside a graph capture: the list is baked into
+// the captured launch); longer lists are copied to stream-ordered scratch first.
 #include <atomic>
 
 #include "ew_kernel.cuh"
@@ -52,8 +52,10 @@ struct IsParams {
     int* err;                // device error word
     int nidx;                // indices held inline (0: use idx)
     const int64_t* idx;      // device copy of the indices (long lists)
-    int64_t inl[kIdxInline];
+    int32_t inl[kIdxInline];  // inline indices (int32: the parameter block stays below 4 KB)
 };
+
+static_assert(sizeof(IsParams) < 4096, "the kernel parameter block stays within 4 KB");
 
 template <typename W>
 __global__ void __launch_bounds__(kIsThreads)
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(kBulkThreads)
 #pragma unroll
             for (int u = 0; u < kIsUnroll; ++u) {
                 const int64_t k = k0 + (int64_t)u * kBulkThreads;
-                if (k < n0) v[u] = row[p.idx_smem ? (int64_t)sidx[k] : (p.nidx ? p.inl[k] : p.idx[k])];
+                if (k < n0) v[u] = row[p.idx_smem ? (int64_t)sidx[k] : (p.nidx ? (int64_t)p.inl[k] : p.idx[k])];
             }
 #pragma unroll
             for (int u = 0; u < kIsUnroll; ++u) {
@@ -458,9 +460,9 @@ int rstsr_cuda_index_select(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_
 
     int64_t* dev_idx = nullptr;
     if (p.axis_dim >= 0) {
-        if (nindices <= kIdxInline) {
+        if (nindices <= kIdxInline && La.shape[axis] <= INT32_MAX) {
             p.nidx = (int)nindices;
-            for (int64_t k = 0; k < nindices; ++k) p.inl[k] = (int64_t)indices[k];
+            for (int64_t k = 0; k < nindices; ++k) p.inl[k] = (int32_t)indices[k];
         } else {
             if (ctx->capturing)
                 return fail(RSTSR_ERR_UNIMPLEMENTED,
