@@ -29,6 +29,9 @@ int after_launch(rstsr_ctx* ctx, const char* name) {
 
 int enter(rstsr_ctx* ctx) {
     if (!ctx) return fail(RSTSR_ERR_INVALID_VALUE, "null context");
+    // a failed call whose status nobody read (a destructor's, another
+    // library's on this thread) must not be reported as this call's launch error
+    (void)cudaGetLastError();
     int cur = -1;
     RSTSR_CUDA_TRY(cudaGetDevice(&cur));
     if (cur != ctx->device) RSTSR_CUDA_TRY(cudaSetDevice(ctx->device));
