@@ -28,6 +28,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -270,8 +271,10 @@ def run_gpu(args):
         wl.step()
     barrier()
     l0 = dev.launch_count()
-    clocks = ClockSampler(str(ROOT / "gpurun_out" / f"clocks_r{rank}.csv")) if rank == 0 else None
-    (ROOT / "gpurun_out").mkdir(exist_ok=True)
+    # the clock samples (summarised in the JSON line) go to RSTSR_BENCH_OUT, else the temp directory
+    out_dir = Path(os.environ.get("RSTSR_BENCH_OUT", tempfile.gettempdir()))
+    out_dir.mkdir(parents=True, exist_ok=True)
+    clocks = ClockSampler(str(out_dir / f"clocks_r{rank}.csv")) if rank == 0 else None
     if clocks:
         clocks.__enter__()
         time.sleep(0.3)  # let the sampler start before the timed region

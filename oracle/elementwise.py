@@ -1,6 +1,6 @@
 """numpy restatement of the reference's element-wise operator semantics
-(TEST INFRASTRUCTURE ONLY: the checker of the device kernels, never the
-product). Each function follows the closure the reference applies per element:
+(TEST INFRASTRUCTURE ONLY: the results the device kernels are compared with,
+never the product). Each function follows the closure the reference applies per element:
 
   round        Rust f64::round (half away from zero), auto_impl/op_binary_common.rs:30
   sign         ExtNum::ext_sign, rstsr-dtype-traits/src/ext_num.rs:83-89, :125-134, :166-178

@@ -1,8 +1,8 @@
 /*
  * rstsr_oracle.c -- CPU restatement of the reference's hot-path semantics.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker for the CUDA backend and
- * the timed CPU baseline of the benchmark; the product never links or calls
+ * TEST INFRASTRUCTURE ONLY. This file gives the results the CUDA backend is
+ * compared with and the timed CPU baseline of the benchmark; the product never links or calls
  * it. It restates, in plain C over explicit (shape, stride, offset) layouts:
  *
  *   assign            rstsr-native-impl/src/cpu_serial/assignment.rs:95-153
