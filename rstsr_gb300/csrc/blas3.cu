@@ -12,10 +12,11 @@
 //    unpack with symmetry Sy) into scratch, then one matmul with alpha / beta;
 //  * TRSM: side R becomes side L on the transposed views and op(A) = A^T a
 //    transposed view of A, so only L X = B (forward) and U X = B (backward)
-//    remain; they run in blocks of kTrsmBlock rows: a small kernel solves the
-//    diagonal block in the operands' own precision (one thread per right-hand
-//    side column, the block of A in shared memory), and the rows below (above)
-//    are updated by one split-GEMM matmul B' -= A' X with alpha = -1, beta = 1.
+//    remain; they are solved by recursive halving down to blocks of
+//    kTrsmBlock rows: a small kernel solves each diagonal block in the
+//    operands' own precision (one thread per right-hand side column, the block
+//    of A in shared memory), and between the halves one split-GEMM matmul
+//    B' -= A' X (alpha = -1, beta = 1) updates the half still to solve.
 #include "ew_kernel.cuh"
 
 namespace rstsr {
@@ -263,10 +264,12 @@ int rstsr_cuda_trsm(rstsr_ctx* ctx, rstsr_order order, char side, char uplo, cha
     if (alpha != 1.0)
         rc = rstsr_cuda_binary_scalar(ctx, RSTSR_OP_MUL, t, b, &lb_full, b, &lb_full, scalar_of(t, alpha, &d, &f), 0);
     if (rc != RSTSR_OK) return rc;
-    const int64_t nblk = (rows + kTrsmBlock - 1) / kTrsmBlock;
-    for (int64_t q = 0; q < nblk; ++q) {
-        const int64_t blk = lower ? q : nblk - 1 - q;
-        const int64_t r0 = blk * kTrsmBlock, r1 = std::min(rows, r0 + kTrsmBlock);
+    // Recursive halving (split points on kTrsmBlock boundaries): solve one half,
+    // update the other with one GEMM of K = that half, solve the other half. The
+    // same flops as a block-by-block sweep, but in GEMMs weighted towards large K
+    // (one of K = rows / 2, two of rows / 4, ...), which the split GEMM runs far
+    // more efficiently than many K = kTrsmBlock updates.
+    auto solve_block = [&](int64_t r0, int64_t r1) -> int {
         const Layout Ad = sub_view(A, r0, r1, r0, r1), Bd = sub_view(B, r0, r1, 0, cols);
         const unsigned grid = (unsigned)((cols + 255) / 256);
         if (t == RSTSR_F64)
@@ -277,15 +280,50 @@ int rstsr_cuda_trsm(rstsr_ctx* ctx, rstsr_order order, char side, char uplo, cha
             trsm_diag_kernel<float><<<grid, 256, 0, ctx->stream>>>(
                 (const float*)a + Ad.offset, Ad.stride[0], Ad.stride[1], (float*)b + Bd.offset, Bd.stride[0],
                 Bd.stride[1], (int)(r1 - r0), cols, lower ? 1 : 0, unit ? 1 : 0);
-        RSTSR_TRY(after_launch(ctx, "trsm_diag_kernel"));
-        // the rows still to solve: B' -= A' X
-        const int64_t u0 = lower ? r1 : 0, u1 = lower ? rows : r0;
-        if (u1 > u0) {
-            const Layout Bu = sub_view(B, u0, u1, 0, cols), Au = sub_view(A, u0, u1, r0, r1);
-            rstsr_layout l0 = Bu.to_abi(), l1 = Au.to_abi(), l2 = Bd.to_abi();
-            rc = rstsr_cuda_matmul(ctx, t, b, &l0, a, &l1, b, &l2, -1.0, 1.0, RSTSR_ROW_MAJOR, opts);
-            if (rc != RSTSR_OK) return rc;
+        return after_launch(ctx, "trsm_diag_kernel");
+    };
+    // B[u0:u1] -= A[u0:u1, s0:s1] X[s0:s1]
+    auto update = [&](int64_t u0, int64_t u1, int64_t s0, int64_t s1) -> int {
+        const Layout Bu = sub_view(B, u0, u1, 0, cols), Au = sub_view(A, u0, u1, s0, s1);
+        const Layout Bs = sub_view(B, s0, s1, 0, cols);
+        rstsr_layout l0 = Bu.to_abi(), l1 = Au.to_abi(), l2 = Bs.to_abi();
+        return rstsr_cuda_matmul(ctx, t, b, &l0, a, &l1, b, &l2, -1.0, 1.0, RSTSR_ROW_MAJOR, opts);
+    };
+    // an explicit stack of row ranges (depth log2(rows / kTrsmBlock)); a range
+    // is pushed with phase 0 (split it) and revisited with phase 1 (update
+    // between its halves, then its second half)
+    struct Frame {
+        int64_t r0, r1, mid;
+        int phase;
+    };
+    std::vector<Frame> stack;
+    stack.push_back({0, rows, 0, 0});
+    while (!stack.empty()) {
+        Frame& f = stack.back();
+        if (f.r1 - f.r0 <= kTrsmBlock) {
+            const int64_t r0 = f.r0, r1 = f.r1;
+            stack.pop_back();
+            RSTSR_TRY(solve_block(r0, r1));
+            continue;
         }
+        if (f.phase == 0) {
+            const int64_t half = (f.r1 - f.r0 + 1) / 2;
+            f.mid = f.r0 + (half + kTrsmBlock - 1) / kTrsmBlock * kTrsmBlock;
+            f.phase = 1;
+            // lower: the top half first; upper: the bottom half first
+            const Frame first = lower ? Frame{f.r0, f.mid, 0, 0} : Frame{f.mid, f.r1, 0, 0};
+            stack.push_back(first);
+            continue;
+        }
+        // phase 1: the first half is solved; update the second half and solve it
+        const int64_t r0 = f.r0, r1 = f.r1, mid = f.mid;
+        stack.pop_back();
+        if (lower)
+            rc = update(mid, r1, r0, mid);
+        else
+            rc = update(r0, mid, mid, r1);
+        if (rc != RSTSR_OK) return rc;
+        stack.push_back(lower ? Frame{mid, r1, 0, 0} : Frame{r0, mid, 0, 0});
     }
     (void)es;
     return RSTSR_OK;
