@@ -125,3 +125,39 @@ def test_contiguity_flags(built_lib):
     assert built_lib.rstsr_cuda_layout_flags(C.byref(L((2, 3), (3, 1)))) & 1
     assert built_lib.rstsr_cuda_layout_flags(C.byref(L((2, 3), (1, 2)))) & 2
     assert built_lib.rstsr_cuda_layout_flags(C.byref(L((2, 3), (6, 2)))) & 3 == 0
+
+
+def test_reduce_output_dtypes_follow_reference(built_lib):
+    """Element type of each reduction's result: T for sum/min/max/prod, T (real) for
+    mean/var/std/l2_norm on float types, usize for count_nonzero and for the sum of a
+    bool array, bool for all/any on bool arrays (the TOut of
+    rstsr-core/src/feature_rayon/auto_impl/reduction.rs:7-716); undefined pairs are
+    InvalidValue errors."""
+    from rstsr_gb300._lib import RED
+
+    F64, F32, F16, BF16, I8, I16, I32, I64, U8, U16, U32, U64, BOOL = range(13)
+    floats = (F64, F32, F16, BF16)
+    ints = (I8, I16, I32, I64, U8, U16, U32, U64)
+
+    def out(op, t):
+        r = C.c_int(-1)
+        rc = built_lib.rstsr_cuda_reduce_out_dtype(RED[op], t, C.byref(r))
+        return r.value if rc == 0 else ("err", rc)
+
+    for t in floats + ints:
+        for op in ("sum", "min", "max", "prod"):
+            assert out(op, t) == t, (op, t)
+        assert out("count_nonzero", t) == U64
+        assert out("all", t) == ("err", 2) and out("any", t) == ("err", 2)
+    for t in floats:
+        for op in ("mean", "var", "std", "l2_norm"):
+            assert out(op, t) == t, (op, t)
+    for t in ints:
+        for op in ("mean", "var", "std", "l2_norm"):
+            assert out(op, t) == ("err", 2), (op, t)
+    assert out("sum", BOOL) == U64
+    assert out("count_nonzero", BOOL) == U64
+    assert out("all", BOOL) == BOOL and out("any", BOOL) == BOOL
+    for op in ("min", "max", "prod", "mean"):
+        assert out(op, BOOL) == ("err", 2), op
+    assert out("sum", 99) == ("err", 2)
