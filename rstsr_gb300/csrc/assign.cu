@@ -344,6 +344,8 @@ static int copy_dispatch(rstsr_ctx* ctx, rstsr_dtype tc, rstsr_dtype ta, const I
         }
     }
     if (sp.size == 0) return RSTSR_OK;
+    if (!inner_extents_fit_u32(sp))
+        return fail(RSTSR_ERR_UNIMPLEMENTED, "casting copy: an inner extent of 2^32 or more elements");
     CastParams p;
     memset(&p, 0, sizeof(p));
     p.dims = make_dev_dims(sp);

@@ -100,6 +100,16 @@ struct DevDims {
 };
 DevDims make_dev_dims(const IterSpace& sp);
 
+// DevDims holds 32-bit extents: the index decomposition (both the 32-bit and
+// the 64-bit form) divides by every extent but the outermost, which is only
+// multiplied, so each of those must be below 2^32. Always true below 2^31
+// elements; false only for a non-collapsible inner extent of 2^32 or more.
+inline bool inner_extents_fit_u32(const IterSpace& sp) {
+    for (int i = 0; i + 1 < sp.ndim; ++i)
+        if (sp.shape[i] > (int64_t)UINT32_MAX) return false;
+    return true;
+}
+
 // ---- dtype helpers ----
 template <typename T> struct DT;
 template <> struct DT<double> { static constexpr rstsr_dtype v = RSTSR_F64; };

@@ -166,6 +166,8 @@ template <typename TO, typename TI, int NIN, typename F>
 static int launch_ew(rstsr_ctx* ctx, const IterSpace& sp, void* out, const EwInput* in, F f,
                      const char* name) {
     if (sp.size == 0) return RSTSR_OK;
+    if (!inner_extents_fit_u32(sp))
+        return fail(RSTSR_ERR_UNIMPLEMENTED, "element-wise kernel: an inner extent of 2^32 or more elements");
     EwParams<NIN> p;
     memset(&p, 0, sizeof(p));
     p.dims = make_dev_dims(sp);
