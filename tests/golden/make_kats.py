@@ -1,4 +1,5 @@
-"""Writes reference_kats.json: known-answer cases transcribed from the
+"""Writes reference_kats.json (and the tri_index, contraction and elementwise
+fixtures beside it): known-answer cases transcribed from the
 reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
 
 Each case names the file:line it comes from. Integer literals in the
@@ -7,6 +8,7 @@ ranges in these tests. Run:  python tests/golden/make_kats.py
 """
 
 import json
+import math
 from pathlib import Path
 
 B3 = [[3, 6, 9], [4, 10, 5], [8, 3, 2]]
@@ -230,6 +232,57 @@ CONTRACTION_CASES = [
          a=[[1, 2], [3, 4]], b=[[5, 6], [7, 8]], expect=[17, 53]),
 ]
 
+# Element-wise family (comparisons, maximum / minimum, unary math, classification).
+# Non-finite values and negative zero are written as strings ("nan", "inf", "-inf",
+# "-0.0") so the file stays plain JSON. `cmp`: "exact" for the reference's `to_vec()`
+# equality, "bits" for exact values including the sign of zero and NaN-ness, "close"
+# for its `assert_equal` (rt::allclose, rtol 1e-5, atol 1e-8).
+_CMP = "rstsr-core/tests/core_func/operators/test_comparison.rs"
+_UM = "rstsr-core/tests/core_func/math/test_unary_math.rs"
+ELEMENTWISE_CASES = [
+    *[
+        dict(src=f"{_CMP}:{line}", op=op, dtype="i32", a=[1, 2, 3, 4], b=[2, 2, 2, 2], expect=e, cmp="exact")
+        for op, line, e in [
+            ("gt", 30, [False, False, True, True]),
+            ("ge", 32, [False, True, True, True]),
+            ("lt", 34, [True, False, False, False]),
+            ("le", 36, [True, True, False, False]),
+            ("eq", 38, [False, True, False, False]),
+            ("ne", 40, [True, False, True, True]),
+        ]
+    ],
+    dict(src=f"{_CMP}:58-61", op="maximum", dtype="i32", a=[1, 5, 3], b=[4, 2, 6], expect=[4, 5, 6], cmp="close"),
+    dict(src=f"{_CMP}:58-63", op="minimum", dtype="i32", a=[1, 5, 3], b=[4, 2, 6], expect=[1, 2, 3], cmp="close"),
+    dict(src=f"{_UM}:27-28", op="abs", dtype="i32", a=[-1, 2, -3], expect=[1, 2, 3], cmp="close"),
+    dict(src=f"{_UM}:31-32", op="sqrt", dtype="f64", a=[0.0, 1.0, 4.0, 9.0], expect=[0.0, 1.0, 2.0, 3.0], cmp="close"),
+    dict(src=f"{_UM}:35-36", op="sign", dtype="f64", a=[-2.0, 0.0, 3.0], expect=[-1.0, 0.0, 1.0], cmp="close"),
+    dict(src=f"{_UM}:39-40", op="sign", dtype="i32", a=[-2, 0, 3], expect=[-1, 0, 1], cmp="exact"),
+    dict(src=f"{_UM}:43-44", op="sign", dtype="u8", a=[0, 5], expect=[0, 1], cmp="exact"),
+    dict(src=f"{_UM}:47-48", op="floor", dtype="f64", a=[-1.5, 0.5, 2.4], expect=[-2.0, 0.0, 2.0], cmp="close"),
+    dict(src=f"{_UM}:47-49", op="ceil", dtype="f64", a=[-1.5, 0.5, 2.4], expect=[-1.0, 1.0, 3.0], cmp="close"),
+    dict(src=f"{_UM}:47-50", op="trunc", dtype="f64", a=[-1.5, 0.5, 2.4], expect=[-1.0, 0.0, 2.0], cmp="close"),
+    dict(src=f"{_UM}:62-69", op="sign", dtype="f64", a=["nan", "inf", "-inf", "-0.0", 0.0],
+         expect=["nan", 1.0, -1.0, 0.0, 0.0], cmp="bits"),
+    dict(src=f"{_UM}:87-93", op="exp", dtype="f64", a=[0.0, 1.0, 2.0], expect=[1.0, math.e, math.e * math.e],
+         cmp="close"),
+    dict(src=f"{_UM}:87-95", op="log", dtype="f64", a=[1.0, math.e, math.e * math.e], expect=[0.0, 1.0, 2.0],
+         cmp="close"),
+    dict(src=f"{_UM}:98-99", op="sin", dtype="f64", a=[0.0, math.pi / 2, math.pi], expect=[0.0, 1.0, 0.0],
+         cmp="close"),
+    dict(src=f"{_UM}:98-100", op="cos", dtype="f64", a=[0.0, math.pi / 2, math.pi], expect=[1.0, 0.0, -1.0],
+         cmp="close"),
+    dict(src=f"{_UM}:103-105", op="tanh", dtype="f64", a=[-1.0, 0.0, 1.0],
+         expect=[-math.tanh(1.0), 0.0, math.tanh(1.0)], cmp="close"),
+    *[
+        dict(src=f"{_UM}:{line}", op=op, dtype="f64", a=[0.0, "nan", "inf", "-inf"], expect=e, cmp="exact")
+        for op, line, e in [
+            ("isnan", "122-123", [False, True, False, False]),
+            ("isfinite", "122-124", [True, False, False, False]),
+            ("isinf", "122-125", [False, False, True, True]),
+        ]
+    ],
+]
+
 
 def main() -> None:
     here = Path(__file__).resolve().parent
@@ -242,6 +295,9 @@ def main() -> None:
     out = here / "contraction_kats.json"
     out.write_text(json.dumps(CONTRACTION_CASES, indent=1) + "\n")
     print(f"wrote {len(CONTRACTION_CASES)} cases to {out}")
+    out = here / "elementwise_kats.json"
+    out.write_text(json.dumps(ELEMENTWISE_CASES, indent=1) + "\n")
+    print(f"wrote {len(ELEMENTWISE_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
