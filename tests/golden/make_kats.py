@@ -1,5 +1,5 @@
-"""Writes reference_kats.json (and the tri_index, contraction and elementwise
-fixtures beside it): known-answer cases transcribed from the
+"""Writes reference_kats.json and the fixtures beside it (tri_index,
+contraction, elementwise, broadcast): known-answer cases transcribed from the
 reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
 
 Each case names the file:line it comes from. Integer literals in the
@@ -284,6 +284,43 @@ ELEMENTWISE_CASES = [
 ]
 
 
+# broadcast_shapes: the shape rule the element-wise operators broadcast by
+# (order "C" aligns trailing axes, "F" leading axes); expect None = an error.
+_BS = "rstsr-core/tests/core_func/manipulation/test_broadcast_shapes.rs"
+BROADCAST_CASES = [
+    *[
+        dict(src=f"{_BS}:18-80", order="C", shapes=s, expect=e)
+        for s, e in [
+            ([], []), ([[]], []), ([[7]], [7]), ([[1, 2], [2]], [1, 2]), ([[1, 1]], [1, 1]),
+            ([[1, 1], [3, 4]], [3, 4]), ([[6, 7], [5, 6, 1], [7], [5, 1, 7]], [5, 6, 7]), ([[5, 6, 1]], [5, 6, 1]),
+            ([[1, 3], [3, 1]], [3, 3]), ([[1, 0], [0, 0]], [0, 0]), ([[0, 1], [0, 0]], [0, 0]),
+            ([[1, 0], [0, 1]], [0, 0]), ([[1, 1], [0, 0]], [0, 0]), ([[1, 1], [1, 0]], [1, 0]),
+            ([[1, 1], [0, 1]], [0, 1]), ([[], [0]], [0]), ([[0], [0, 0]], [0, 0]), ([[0], [0, 1]], [0, 0]),
+            ([[1], [0, 0]], [0, 0]), ([[], [0, 0]], [0, 0]), ([[1, 1], [0]], [1, 0]), ([[1], [0, 1]], [0, 1]),
+            ([[1], [1, 0]], [1, 0]), ([[], [1, 0]], [1, 0]), ([[], [0, 1]], [0, 1]), ([[1], [3]], [3]),
+            ([[2], [3, 2]], [3, 2]),
+        ]
+    ],
+    dict(src=f"{_BS}:84-87", order="C", shapes=[[1, 2]] * 32, expect=[1, 2]),
+    dict(src=f"{_BS}:89-92", order="C", shapes=[[1, 2]] * 100, expect=[1, 2]),
+    dict(src=f"{_BS}:94-97", order="C", shapes=[[2]] * 32, expect=[2]),
+    *[
+        dict(src=f"{_BS}:106-123", order="C", shapes=s, expect=None)
+        for s in [
+            [[3], [4]], [[2, 3], [2]], [[3], [3], [4]], [[1, 3, 4], [2, 3, 3]], [[1, 2], [3, 1], [3, 2], [10, 5]],
+            [[2], [2, 3]],
+        ]
+    ],
+    dict(src=f"{_BS}:126-130", order="C", shapes=[[2]] * 32 + [[3]] * 32, expect=None),
+    dict(src=f"{_BS}:167-171", order="C", shapes=[[2]] * 32 + [[]], expect=[2]),
+    dict(src=f"{_BS}:190-192", order="F", shapes=[[1, 6, 1, 8], [5, 1, 7]], expect=[5, 6, 7, 8]),
+    dict(src=f"{_BS}:198-200", order="F", shapes=[[4, 5], [4]], expect=[4, 5]),
+    dict(src=f"{_BS}:206-208", order="F", shapes=[[5, 3, 15], [5, 1, 15]], expect=[5, 3, 15]),
+    dict(src=f"{_BS}:214-216", order="F", shapes=[[5, 3, 15], [5, 3]], expect=[5, 3, 15]),
+    dict(src=f"{_BS}:220-222", order="F", shapes=[[3], [2, 1]], expect=None),
+]
+
+
 def main() -> None:
     here = Path(__file__).resolve().parent
     out = here / "reference_kats.json"
@@ -298,6 +335,9 @@ def main() -> None:
     out = here / "elementwise_kats.json"
     out.write_text(json.dumps(ELEMENTWISE_CASES, indent=1) + "\n")
     print(f"wrote {len(ELEMENTWISE_CASES)} cases to {out}")
+    out = here / "broadcast_kats.json"
+    out.write_text(json.dumps(BROADCAST_CASES, indent=1) + "\n")
+    print(f"wrote {len(BROADCAST_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
