@@ -1,5 +1,5 @@
 """Writes reference_kats.json and the fixtures beside it (tri_index,
-contraction, elementwise, broadcast): known-answer cases transcribed from the
+contraction, elementwise, broadcast, reshape): known-answer cases transcribed from the
 reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
 
 Each case names the file:line it comes from. Integer literals in the
@@ -321,6 +321,27 @@ BROADCAST_CASES = [
 ]
 
 
+# reshape through a copy: the values of a (strided) source walked in C or F
+# order into the target shape (assign_arbitrary). `buf` is the source storage,
+# `view` = (shape, stride, offset) over it; `expect` is indexed [i][j].
+_RS = "rstsr-core/tests/core_func/manipulation/test_reshape.rs"
+_A43 = list(range(1, 13))
+RESHAPE_CASES = [
+    dict(src=f"{_RS}:22-27", buf=_A43, view=[[4, 3], [3, 1], 0], shape=[2, 6], order="C",
+         expect=[[1, 2, 3, 4, 5, 6], [7, 8, 9, 10, 11, 12]]),
+    dict(src=f"{_RS}:30-32", buf=_A43, view=[[4, 3], [3, 1], 0], shape=[3, 4], order="C",
+         expect=[[1, 2, 3, 4], [5, 6, 7, 8], [9, 10, 11, 12]]),
+    dict(src=f"{_RS}:35-37", buf=_A43, view=[[4, 3], [3, 1], 0], shape=[3, 4], order="F",
+         expect=[[1, 10, 8, 6], [4, 2, 11, 9], [7, 5, 3, 12]]),
+    dict(src=f"{_RS}:40-42", buf=_A43, view=[[3, 4], [1, 3], 0], shape=[3, 4], order="C",
+         expect=[[1, 4, 7, 10], [2, 5, 8, 11], [3, 6, 9, 12]]),
+    dict(src=f"{_RS}:55-59", buf=list(range(6)), view=[[6], [1], 0], shape=[2, 3], order="F",
+         expect=[[0, 2, 4], [1, 3, 5]]),
+    dict(src=f"{_RS}:63-67", buf=list(range(1, 9)), view=[[4], [2], 1], shape=[2, 2], order="F",
+         expect=[[2, 6], [4, 8]]),
+]
+
+
 def main() -> None:
     here = Path(__file__).resolve().parent
     out = here / "reference_kats.json"
@@ -338,6 +359,9 @@ def main() -> None:
     out = here / "broadcast_kats.json"
     out.write_text(json.dumps(BROADCAST_CASES, indent=1) + "\n")
     print(f"wrote {len(BROADCAST_CASES)} cases to {out}")
+    out = here / "reshape_kats.json"
+    out.write_text(json.dumps(RESHAPE_CASES, indent=1) + "\n")
+    print(f"wrote {len(RESHAPE_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
