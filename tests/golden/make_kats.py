@@ -1,6 +1,6 @@
 """Writes reference_kats.json and the fixtures beside it (tri_index,
-contraction, elementwise, broadcast, reshape): known-answer cases transcribed from the
-reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
+contraction, elementwise, broadcast, reshape, vecdot): known-answer cases
+transcribed from the reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
 
 Each case names the file:line it comes from. Integer literals in the
 reference's `tensor_from_nested!` are i32; `arange` defaults to i32 for integer
@@ -342,6 +342,22 @@ RESHAPE_CASES = [
 ]
 
 
+# vecdot along one axis with the remaining axes broadcast: `a` / `b` as
+# (start, stop, shape) aranges or explicit nested lists, `a_view` / `b_view` a
+# step-2 slice of the last axis, `axis` counted from the end.
+_VD = "rstsr-core/tests/core_func/linalg/test_vecdot.rs"
+VECDOT_CASES = [
+    dict(src=f"{_VD}:25-29", a=[0, 6, [2, 3]], b=[0, 3, [1, 3]], axis=-1, expect=[5, 14]),
+    dict(src=f"{_VD}:31-34", a=[0, 6, [2, 3]], b=[0, 3, [1, 3]], transpose=True, axis=-2, expect=[5, 14]),
+    dict(src=f"{_VD}:49-53", a=[0, 4, [2, 1, 2]], b=[0, 4, [1, 2, 2]], axis=-1, expect=[[1, 3], [3, 13]]),
+    dict(src=f"{_VD}:58-61", a=[0, 4, [2, 1, 2]], b=[0, 4, [2, 2]], axis=-1, expect=[[1, 3], [3, 13]]),
+    dict(src=f"{_VD}:144-149", a=[0, 0, [0]], b=[0, 0, [0]], axis=-1,
+         expect=0),
+    dict(src=f"{_VD}:160-169", a=[0, 12, [3, 4]], b=[8, 20, [3, 4]], a_view="step2", b_view="step2", axis=-1,
+         expect=[20, 132, 308]),
+]
+
+
 def main() -> None:
     here = Path(__file__).resolve().parent
     out = here / "reference_kats.json"
@@ -362,6 +378,9 @@ def main() -> None:
     out = here / "reshape_kats.json"
     out.write_text(json.dumps(RESHAPE_CASES, indent=1) + "\n")
     print(f"wrote {len(RESHAPE_CASES)} cases to {out}")
+    out = here / "vecdot_kats.json"
+    out.write_text(json.dumps(VECDOT_CASES, indent=1) + "\n")
+    print(f"wrote {len(VECDOT_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
