@@ -88,7 +88,11 @@ typedef struct rstsr_ctx rstsr_ctx;
 
 /* Device construction (the DeviceCpuRayon/DeviceOpenBLAS `new` pattern,
  * rstsr-core/src/feature_rayon/device.rs:41-129): binds a CUDA device, an
- * owned non-blocking stream and a stream-ordered memory pool. */
+ * owned non-blocking stream and a stream-ordered memory pool. The first call
+ * in a process loads the GEMM autotune table named by the environment variable
+ * RSTSR_CUDA_AUTOTUNE_TABLE (as rstsr_cuda_autotune_load) when it is set; a
+ * missing or malformed file makes every context creation fail with that
+ * load's error. */
 int rstsr_cuda_ctx_create(int32_t device, rstsr_ctx** out);
 int rstsr_cuda_ctx_destroy(rstsr_ctx* ctx);
 /* Blocks until all work queued on the context's stream is done. */

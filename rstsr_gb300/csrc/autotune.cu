@@ -4,10 +4,14 @@
 // consults (tune_config). The table is saved and loaded as text, one entry a
 // line:
 //   <mode: ozaki | bf16x3> <slices> <log2 m> <log2 n> <log2 k> <kt> <group>
-// with the log2 values rounded up. The reference has no counterpart: rstsr's
-// CPU GEMMs take their blocking from faer / the BLAS library.
+// with the log2 values rounded up. A process started with
+// RSTSR_CUDA_AUTOTUNE_TABLE=<file> has that file loaded by its first context
+// creation, which fails with the load's error if the file is missing or
+// malformed. The reference has no counterpart: rstsr's CPU GEMMs take their
+// blocking from faer / the BLAS library.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -62,6 +66,19 @@ __global__ void fill_uniform_kernel(T* __restrict__ x, int64_t n, uint32_t seed)
 }
 
 }  // namespace
+
+int load_env_table() {
+    static std::once_flag once;
+    static int status = RSTSR_OK;
+    static std::string msg;
+    std::call_once(once, [] {
+        const char* path = std::getenv("RSTSR_CUDA_AUTOTUNE_TABLE");
+        if (!path || !*path) return;
+        status = rstsr_cuda_autotune_load(path);
+        if (status != RSTSR_OK) msg = rstsr_cuda_last_error();
+    });
+    return status == RSTSR_OK ? RSTSR_OK : fail(status, "RSTSR_CUDA_AUTOTUNE_TABLE: " + msg);
+}
 
 TuneConfig tune_config(SplitMode mode, int slices, int64_t M, int64_t N, int64_t K) {
     if (g_force.kt) return g_force;

@@ -44,6 +44,10 @@ int after_launch(rstsr_ctx* ctx, const char* name);
 // Validate a context pointer and make its device current.
 int enter(rstsr_ctx* ctx);
 
+// Loads the GEMM autotune table named by RSTSR_CUDA_AUTOTUNE_TABLE, once per
+// process (no-op when unset); the status of that load on every call.
+int load_env_table();
+
 // Scratch memory from the context pool (stream-ordered).
 int scratch_alloc(rstsr_ctx* ctx, size_t bytes, void** p);
 void scratch_free(rstsr_ctx* ctx, void* p);

@@ -155,6 +155,7 @@ int rstsr_cuda_ctx_create(int32_t device, rstsr_ctx** out) {
     clear_error();
     if (!out) return fail(RSTSR_ERR_INVALID_VALUE, "null output pointer");
     *out = nullptr;
+    if (int s = load_env_table()) return s;
     int ndev = 0;
     RSTSR_CUDA_TRY(cudaGetDeviceCount(&ndev));
     if (device < 0 || device >= ndev)

@@ -40,3 +40,48 @@ def test_malformed_file_is_rejected_and_table_kept(built_lib, tmp_path, bad):
 def test_missing_file_is_an_error(built_lib, tmp_path):
     with pytest.raises(rt.RstsrError):
         rt.autotune_load(tmp_path / "does_not_exist.txt")
+
+
+def _in_child(tmp_path, env_value, body):
+    """Run `body` in a fresh interpreter (the environment table loads once per
+    process) with RSTSR_CUDA_AUTOTUNE_TABLE set; return its stdout."""
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    env = dict(os.environ, RSTSR_CUDA_AUTOTUNE_TABLE=str(env_value), PYTHONPATH=str(root))
+    script = "import rstsr_gb300 as rt\n" + body
+    res = subprocess.run([sys.executable, "-c", script], cwd=root, env=env, capture_output=True, text=True,
+                         timeout=120)
+    assert res.returncode == 0, res.stderr
+    return res.stdout
+
+
+def test_environment_table_is_loaded_by_the_first_context(built_lib, tmp_path):
+    table = tmp_path / "env_table.txt"
+    table.write_text("ozaki 7 12 12 9 32 8\nbf16x3 3 11 11 11 16 4\n")
+    out = tmp_path / "saved.txt"
+    body = (
+        "try:\n    rt.DeviceCuda(0)\nexcept rt.RstsrError:\n    pass  # no GPU here: the table loads first\n"
+        f"rt.autotune_save({str(out)!r})\n"
+    )
+    _in_child(tmp_path, table, body)
+    assert entries(out.read_text()) == entries(table.read_text())
+
+
+@pytest.mark.parametrize("content", ["ozaki 7 12 12 9 24 8\n", None])
+def test_bad_environment_table_fails_context_creation(built_lib, tmp_path, content):
+    table = tmp_path / "env_table.txt"
+    if content is not None:
+        table.write_text(content)
+    body = (
+        "for _ in range(2):\n"
+        "    try:\n        rt.DeviceCuda(0)\n        print('created')\n"
+        "    except rt.RstsrError as e:\n        print(e.kind, str(e))\n"
+    )
+    lines = _in_child(tmp_path, table, body).splitlines()
+    assert len(lines) == 2 and all("RSTSR_CUDA_AUTOTUNE_TABLE" in line for line in lines), lines
+    want = "InvalidValue" if content is not None else "RuntimeError"
+    assert all(line.startswith(want) for line in lines), lines
