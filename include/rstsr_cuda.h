@@ -166,6 +166,36 @@ int rstsr_cuda_assign_arbitrary(rstsr_ctx* ctx, void* c, const rstsr_layout* lc,
 int rstsr_cuda_fill(rstsr_ctx* ctx, void* c, const rstsr_layout* lc, rstsr_dtype tc,
                     const void* value);
 
+/* --------------------------------------------------------------- creation */
+
+/* DeviceCreationArangeAPI::arange_impl (rstsr-core/src/storage/creation.rs:51-53;
+ * rayon device rstsr-core/src/feature_rayon/auto_impl/creation.rs:74-86).
+ * Host-only: the number of elements arange(start, end, step) has for element
+ * type t (start, end, step point at one HOST element of type t each): f64 / f32
+ * n = ceil((end - start) / step) in f64, i32 / i64 / u32 / u64 the same through
+ * isize, each dropping a last element not strictly inside the interval
+ * (rstsr-native-impl/src/cpu_rayon/creation.rs:8-55); i8 / i16 / u8 / u16 (and u64
+ * values above isize::MAX) count the repeated addition `current < end`
+ * (cpu_serial/creation.rs:7-19). A zero step is InvalidValue; ranges the
+ * reference's repeated addition never finishes (it wraps, runs away from the
+ * end or stops changing) are ValueOutOfRange; f16 / bf16 / bool and a NaN step
+ * are UnImplemented. */
+int rstsr_cuda_arange_len(rstsr_dtype t, const void* start, const void* end, const void* step, int64_t* n);
+/* Writes the n values of that arange to c[0..n): start + i * step (f64 / f32 in
+ * f64 with two roundings, integers in 64-bit wrapping arithmetic). */
+int rstsr_cuda_arange(rstsr_ctx* ctx, rstsr_dtype t, void* c, int64_t n, const void* start, const void* step);
+/* DeviceCreationComplexFloatAPI::linspace_impl (creation.rs:41-49; rayon device
+ * rstsr-native-impl/src/cpu_rayon/creation.rs:108-128), f64 / f32: c[i] =
+ * start + i * step in the element type, step = (end - start) / (n - 1), or / n
+ * with endpoint = 0; c[0] = start when n = 1. */
+int rstsr_cuda_linspace(rstsr_ctx* ctx, rstsr_dtype t, void* c, int64_t n, const void* start, const void* end,
+                        int32_t endpoint);
+/* DeviceCreationTriAPI::tril_impl / triu_impl (creation.rs:55-62;
+ * rstsr-native-impl/src/cpu_serial/op_tri.rs:524-591), in place on the last two
+ * axes of lc (ndim >= 2): upper = 0 zeroes j >= i + k + 1 (tril), upper = 1
+ * zeroes j < i + k (triu, clipped to the row). */
+int rstsr_cuda_tril(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc, int64_t k, int32_t upper);
+
 /* ------------------------------------------------------------ elementwise */
 
 /* Binary operators of rstsr-core/src/operators/ops/op_ternary_arithmetic.rs:3-56

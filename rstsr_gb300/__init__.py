@@ -13,6 +13,7 @@ from .tensor import (  # noqa: F401
     DeviceCuda,
     Graph,
     Tensor,
+    arange,
     argreduce_all,
     argreduce_axes,
     asarray,
@@ -33,6 +34,7 @@ from .tensor import (  # noqa: F401
     full,
     index_select,
     isclose,
+    linspace,
     matmul,
     matmul_into,
     pack_tri,
@@ -44,6 +46,8 @@ from .tensor import (  # noqa: F401
     syrk,
     take,
     tensordot,
+    tril,
+    triu,
     trsm,
     to_contig,
     unary,

@@ -163,6 +163,10 @@ _SIGS = {
     "rstsr_cuda_assign": ([_P, _P, _L, _I, _P, _L, _I], C.c_int),
     "rstsr_cuda_assign_arbitrary": ([_P, _P, _L, _I, _P, _L, _I, _I], C.c_int),
     "rstsr_cuda_fill": ([_P, _P, _L, _I, _P], C.c_int),
+    "rstsr_cuda_arange_len": ([_I, _P, _P, _P, C.POINTER(C.c_int64)], C.c_int),
+    "rstsr_cuda_arange": ([_P, _I, _P, C.c_int64, _P, _P], C.c_int),
+    "rstsr_cuda_linspace": ([_P, _I, _P, C.c_int64, _P, _P, C.c_int32], C.c_int),
+    "rstsr_cuda_tril": ([_P, _I, _P, _L, C.c_int64, C.c_int32], C.c_int),
     "rstsr_cuda_binary": ([_P, _I, _I, _P, _L, _P, _L, _P, _L], C.c_int),
     "rstsr_cuda_binary_scalar": ([_P, _I, _I, _P, _L, _P, _L, _P, _I], C.c_int),
     "rstsr_cuda_binary_inplace": ([_P, _I, _I, _P, _L, _P, _L, _I], C.c_int),

@@ -526,6 +526,61 @@ def fill(t: Tensor, value) -> None:
     call("rstsr_cuda_fill", t.device.ctx, C.c_void_p(t.ptr), C.byref(t.layout()), t.dtype_code, s)
 
 
+def arange(start, stop=None, step=1, *, dtype=None, device: DeviceCuda) -> Tensor:
+    """arange_f (rstsr-core/src/tensor/creation.rs:55-110): `arange(stop)`,
+    `arange(start, stop)` or `arange(start, stop, step)`, 1-D; the element type
+    defaults to f64 when a bound is a float, else i64. The length is host
+    arithmetic (rstsr_cuda_arange_len), the values one kernel."""
+    if stop is None:
+        start, stop = 0, start
+    if dtype is None:
+        dtype = np.float64 if any(isinstance(v, float) for v in (start, stop, step)) else np.int64
+    code = dtype if isinstance(dtype, int) else dtype_code(dtype)
+    s, e, st = (_scalar_bytes(v, code) for v in (start, stop, step))
+    n = C.c_int64()
+    call("rstsr_cuda_arange_len", code, s, e, st, C.byref(n))
+    out = empty((n.value,), code, device)
+    if n.value:
+        call("rstsr_cuda_arange", device.ctx, code, C.c_void_p(out.ptr), n.value, s, st)
+    return out
+
+
+def linspace(start, stop, num: int, *, endpoint: bool = True, dtype=np.float64, device: DeviceCuda) -> Tensor:
+    """linspace_f (rstsr-core/src/tensor/creation.rs:760-800): `num` values from
+    `start` to `stop` (f64 / f32), the last one `stop` when `endpoint`."""
+    num = int(num)
+    if num < 0:
+        raise RstsrError(2, "linspace: num must not be negative")
+    code = dtype if isinstance(dtype, int) else dtype_code(dtype)
+    out = empty((num,), code, device)
+    call("rstsr_cuda_linspace", device.ctx, code, C.c_void_p(out.ptr), num, _scalar_bytes(start, code),
+         _scalar_bytes(stop, code), 1 if endpoint else 0)
+    return out
+
+
+def _tri_mask(t: Tensor, k: int, upper: bool, inplace: bool) -> Tensor:
+    out = t
+    if not inplace:
+        out = empty(t.shape, t.dtype_code, t.device, order="C" if t.device.default_order == ROW_MAJOR else "F")
+        assign(out, t)
+    call("rstsr_cuda_tril", t.device.ctx, t.dtype_code, C.c_void_p(out.ptr), C.byref(out.layout()), int(k),
+         1 if upper else 0)
+    return out
+
+
+def tril(t: Tensor, k: int = 0, inplace: bool = False) -> Tensor:
+    """tril_f (rstsr-core/src/tensor/creation.rs:1451-1560): zeros above the k-th
+    diagonal of the last two axes, in a contiguous copy (default order) or in
+    place."""
+    return _tri_mask(t, k, False, inplace)
+
+
+def triu(t: Tensor, k: int = 0, inplace: bool = False) -> Tensor:
+    """triu_f (rstsr-core/src/tensor/creation.rs:1640-1750): zeros below the k-th
+    diagonal of the last two axes."""
+    return _tri_mask(t, k, True, inplace)
+
+
 def _scalar_bytes(value, code: int):
     if code == _lib.BF16:
         f = np.float32(value).view(np.uint32)

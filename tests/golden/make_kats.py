@@ -1,5 +1,5 @@
 """Writes reference_kats.json and the fixtures beside it (tri_index,
-contraction, elementwise, broadcast, reshape, vecdot): known-answer cases
+contraction, elementwise, broadcast, reshape, vecdot, creation): known-answer cases
 transcribed from the reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
 
 Each case names the file:line it comes from. Integer literals in the
@@ -358,6 +358,48 @@ VECDOT_CASES = [
 ]
 
 
+# Creation: arange (`args` = [stop] | [start, stop] | [start, stop, step]),
+# linspace (`args` = [start, stop, num], `endpoint`), tril / triu (`k`).
+# `expect` values, `expect_len`, `last_close` (|last - v| < 1e-9),
+# `last_below` (last < v) or `error` (the reference's error kind).
+_AR = "rstsr-core/tests/core_func/creation/test_arange.rs"
+_LS = "rstsr-core/tests/core_func/creation/test_linspace.rs"
+_TT = "rstsr-core/tests/core_func/creation/test_tril_triu.rs"
+_TSER = "rstsr-core/src/device_cpu_serial/creation.rs"
+_ONES2 = [[1, 1], [1, 1]]
+_ONES3 = [[1, 1, 1], [1, 1, 1], [1, 1, 1]]
+_A3D = [[[1, 1], [1, 1]], [[1, 1], [1, 0]], [[1, 1], [0, 0]]]
+_M9 = [[1, 2, 3], [4, 5, 6], [7, 8, 9]]
+CREATION_CASES = [
+    dict(src=f"{_AR}:26-28", op="arange", dtype="i32", args=[3], expect_len=3),
+    dict(src=f"{_AR}:27-30", op="arange", dtype="i32", args=[0, 3], expect_len=3),
+    dict(src=f"{_AR}:31-32", op="arange", dtype="i32", args=[3, 9], expect_len=6),
+    dict(src=f"{_AR}:45", op="arange", dtype="i32", args=[0, 10, 0], error="InvalidValue"),
+    dict(src=f"{_AR}:46", op="arange", dtype="f64", args=[0.0, 10.0, 0.0], error="InvalidValue"),
+    dict(src=f"{_AR}:62-63", op="arange", dtype="i32", args=[2, 10], expect=[2, 3, 4, 5, 6, 7, 8, 9]),
+    dict(src=f"{_AR}:65-66", op="arange", dtype="i32", args=[1, 10, 3], expect=[1, 4, 7]),
+    dict(src=f"{_AR}:68-69", op="arange", dtype="i32", args=[10, 0, -2], expect=[10, 8, 6, 4, 2]),
+    dict(src="rstsr-core/src/feature_rayon/auto_impl/creation.rs:126-130", op="linspace", dtype="f64",
+         args=[1.0, 5.0, 5], endpoint=True, expect=[1.0, 2.0, 3.0, 4.0, 5.0]),
+    dict(src=f"{_LS}:23-25", op="linspace", dtype="f64", args=[0.0, 10.0, 50], endpoint=True, expect_len=50),
+    dict(src=f"{_LS}:27-30", op="linspace", dtype="f64", args=[2.0, 10.0, 100], endpoint=True, last_close=10.0),
+    dict(src=f"{_LS}:32-35", op="linspace", dtype="f64", args=[2.0, 10.0, 100], endpoint=False, last_below=10.0),
+    dict(src=f"{_LS}:50-52", op="linspace", dtype="f64", args=[0.0, 1.0, 1], endpoint=True, expect=[0.0]),
+    dict(src=f"{_LS}:69-71", op="linspace", dtype="f64", args=[0.0, 1.0, 5], endpoint=True,
+         expect=[0.0, 0.25, 0.5, 0.75, 1.0]),
+    dict(src=f"{_TT}:26-28", op="tril", dtype="i32", a=_ONES2, k=0, expect=[[1, 0], [1, 1]]),
+    dict(src=f"{_TT}:26-30", op="triu", dtype="i32", a=_ONES2, k=0, expect=[[1, 1], [0, 1]]),
+    dict(src=f"{_TT}:42-47", op="tril", dtype="i32", a=_A3D, k=0,
+         expect=[[[1, 0], [1, 1]], [[1, 0], [1, 0]], [[1, 0], [0, 0]]]),
+    dict(src=f"{_TT}:42-48", op="triu", dtype="i32", a=_A3D, k=0,
+         expect=[[[1, 1], [0, 1]], [[1, 1], [0, 0]], [[1, 1], [0, 0]]]),
+    dict(src=f"{_TT}:60-62", op="tril", dtype="i32", a=_ONES3, k=1, expect=[[1, 1, 0], [1, 1, 1], [1, 1, 1]]),
+    dict(src=f"{_TT}:60-66", op="triu", dtype="i32", a=_ONES3, k=-1, expect=[[1, 1, 1], [1, 1, 1], [0, 1, 1]]),
+    dict(src=f"{_TSER}:160-165", op="tril", dtype="i32", a=_M9, k=-1, expect=[[0, 0, 0], [4, 0, 0], [7, 8, 0]]),
+    dict(src=f"{_TSER}:166-169", op="triu", dtype="i32", a=_M9, k=-1, expect=[[1, 2, 3], [4, 5, 6], [0, 8, 9]]),
+]
+
+
 def main() -> None:
     here = Path(__file__).resolve().parent
     out = here / "reference_kats.json"
@@ -381,6 +423,9 @@ def main() -> None:
     out = here / "vecdot_kats.json"
     out.write_text(json.dumps(VECDOT_CASES, indent=1) + "\n")
     print(f"wrote {len(VECDOT_CASES)} cases to {out}")
+    out = here / "creation_kats.json"
+    out.write_text(json.dumps(CREATION_CASES, indent=1) + "\n")
+    print(f"wrote {len(CREATION_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
