@@ -330,6 +330,13 @@ int rstsr_cuda_compare_scalar(rstsr_ctx* ctx, rstsr_compare_op op, rstsr_dtype t
 int rstsr_cuda_isclose(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layout* lc,
                        const void* a, const rstsr_layout* la, const void* b, const rstsr_layout* lb,
                        double rtol, double atol, int32_t equal_nan);
+/* OpAllCloseAPI::allclose_all (rstsr-core/src/operators/reduction.rs:73-85; rayon
+ * device rstsr-core/src/feature_rayon/auto_impl/reduction.rs:717-749): every
+ * element of a and b (same shape) isclose; the bool is written to HOST memory at
+ * out_host (synchronises). A zero-size operand is InvalidValue, as in the
+ * reference. */
+int rstsr_cuda_allclose_all(rstsr_ctx* ctx, rstsr_dtype t, const void* a, const rstsr_layout* la, const void* b,
+                            const rstsr_layout* lb, double rtol, double atol, int32_t equal_nan, uint8_t* out_host);
 
 /* Fused d = a * b + c (one pass). The reference evaluates `&a * &b + &c` as
  * OpMulAPI::op_mutc_refa_refb (tensor/operators/op_binary_arithmetic.rs:170-213)

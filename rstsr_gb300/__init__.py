@@ -14,6 +14,7 @@ from .tensor import (  # noqa: F401
     Graph,
     Tensor,
     arange,
+    allclose,
     argreduce_all,
     argreduce_axes,
     asarray,

@@ -175,6 +175,7 @@ _SIGS = {
     "rstsr_cuda_compare": ([_P, _I, _I, _P, _L, _P, _L, _P, _L], C.c_int),
     "rstsr_cuda_compare_scalar": ([_P, _I, _I, _P, _L, _P, _L, _P, _I], C.c_int),
     "rstsr_cuda_isclose": ([_P, _I, _P, _L, _P, _L, _P, _L, C.c_double, C.c_double, _I], C.c_int),
+    "rstsr_cuda_allclose_all": ([_P, _I, _P, _L, _P, _L, C.c_double, C.c_double, C.c_int32, C.POINTER(C.c_uint8)], C.c_int),
     "rstsr_cuda_fma": ([_P, _I, _P, _L, _P, _L, _P, _L, _P, _L], C.c_int),
     "rstsr_cuda_reduce_out_dtype": ([_I, _I, C.POINTER(C.c_int)], C.c_int),
     "rstsr_cuda_reduce_all": ([_P, _I, _I, _P, _L, _P], C.c_int),

@@ -3,7 +3,9 @@
 // op_binary_common.rs:94-120), the comparisons OpEqualAPI ... OpLessEqualAPI
 // and OpIsCloseAPI (rstsr-core/src/operators/ops/op_ternary_common.rs:3-100,
 // rstsr-dtype-traits/src/isclose.rs:92-105). They run on the strided
-// element-wise kernel with a bool (byte) output type.
+// element-wise kernel with a bool (byte) output type. OpAllCloseAPI::allclose_all
+// (rstsr-core/src/feature_rayon/auto_impl/reduction.rs:717-749) is isclose into
+// scratch followed by the all-reduction.
 #include "ew_kernel.cuh"
 
 namespace rstsr {
@@ -224,6 +226,29 @@ int rstsr_cuda_isclose(rstsr_ctx* ctx, rstsr_dtype t, void* c, const rstsr_layou
     if (empty) return RSTSR_OK;
     EwInput ins[2] = {{a, nullptr}, {b, nullptr}};
     return dispatch_bool_out<IsCloseF>(ctx, t, sp, c, ins, 2, rtol, atol, (int)(equal_nan != 0));
+}
+
+int rstsr_cuda_allclose_all(rstsr_ctx* ctx, rstsr_dtype t, const void* a, const rstsr_layout* la, const void* b,
+                            const rstsr_layout* lb, double rtol, double atol, int32_t equal_nan, uint8_t* out_host) {
+    clear_error();
+    RSTSR_TRY(enter(ctx));
+    RSTSR_TRY(check_layout(la, "a"));
+    RSTSR_TRY(check_layout(lb, "b"));
+    if (!out_host) return fail(RSTSR_ERR_INVALID_VALUE, "null output");
+    const Layout A = Layout::from_abi(*la), B = Layout::from_abi(*lb);
+    if (A.size() == 0 || B.size() == 0)
+        return fail(RSTSR_ERR_INVALID_VALUE, "zero-size array is not supported for allclose");
+    if (!same_shape(A, B))
+        return fail(RSTSR_ERR_INVALID_LAYOUT, "allclose: a and b differ in shape (broadcast them first)");
+    // the element-wise test into a C-contiguous bool scratch, then the all-reduction
+    const Layout M = Layout::c_contig(A.shape, A.ndim);
+    void* mask = nullptr;
+    RSTSR_TRY(scratch_alloc(ctx, (size_t)M.size(), &mask));
+    const rstsr_layout lm = M.to_abi();
+    int rc = rstsr_cuda_isclose(ctx, t, mask, &lm, a, la, b, lb, rtol, atol, equal_nan);
+    if (rc == RSTSR_OK) rc = rstsr_cuda_reduce_all(ctx, RSTSR_RED_ALL, RSTSR_BOOL, mask, &lm, out_host);
+    scratch_free(ctx, mask);
+    return rc;
 }
 
 }  // extern "C"

@@ -1153,6 +1153,19 @@ def isclose(a: Tensor, b: Tensor, rtol: float = 1.0e-5, atol: float = 1.0e-8, eq
     return out
 
 
+def allclose(a: Tensor, b: Tensor, rtol: float = 1.0e-5, atol: float = 1.0e-8, equal_nan: bool = False) -> bool:
+    """allclose (OpAllCloseAPI::allclose_all): every broadcast element pair
+    isclose; a zero-size operand is an InvalidValue error, as in the reference."""
+    _same_device(a, b)
+    if a.dtype_code != b.dtype_code:
+        raise RstsrError(2, f"dtype mismatch {a.dtype} vs {b.dtype}")
+    la, lb = broadcast_layouts(a, b, a.device.default_order)
+    out = C.c_uint8(0)
+    call("rstsr_cuda_allclose_all", a.device.ctx, a.dtype_code, C.c_void_p(a.ptr), C.byref(la), C.c_void_p(b.ptr),
+         C.byref(lb), float(rtol), float(atol), 1 if equal_nan else 0, C.byref(out))
+    return bool(out.value)
+
+
 # ---------------------------------------------------------- BLAS-3 drivers
 
 
