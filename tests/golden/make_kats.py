@@ -1,6 +1,6 @@
 """Writes reference_kats.json and the fixtures beside it (tri_index,
-contraction, elementwise, broadcast, reshape, vecdot, creation): known-answer cases
-transcribed from the reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
+contraction, elementwise, broadcast, reshape, vecdot, creation, layout):
+known-answer cases transcribed from the reference's own test suite (RESTGroup/rstsr, paths relative to its workspace).
 
 Each case names the file:line it comes from. Integer literals in the
 reference's `tensor_from_nested!` are i32; `arange` defaults to i32 for integer
@@ -400,6 +400,89 @@ CREATION_CASES = [
 ]
 
 
+# Layout algebra (rstsr-common/src/layout): contiguity / preference flags,
+# matmul output layouts and broadcast layouts. Layouts are [shape, stride, offset].
+_LB = "rstsr-common/src/layout/layoutbase.rs"
+_LM = "rstsr-common/src/layout/matmul.rs"
+_BR = "rstsr-common/src/layout/broadcast.rs"
+
+
+def _cs(shape):
+    st, acc = [], 1
+    for d in reversed(shape):
+        st.append(acc)
+        acc *= max(d, 1)
+    return st[::-1]
+
+
+def _fs(shape):
+    st, acc = [], 1
+    for d in shape:
+        st.append(acc)
+        acc *= max(d, 1)
+    return st
+
+
+def _c(shape):
+    return [list(shape), _cs(shape), 0]
+
+
+def _f(shape):
+    return [list(shape), _fs(shape), 0]
+
+
+def _swap(lay, i, j):
+    sh, st, off = [list(x) if isinstance(x, list) else x for x in lay]
+    sh[i], sh[j] = sh[j], sh[i]
+    st[i], st[j] = st[j], st[i]
+    return [sh, st, off]
+
+
+_S357 = [3, 5, 7]
+LAYOUT_CASES = [
+    *[dict(src=f"{_LB}:755-779", op="flag", flag="f_prefer", layout=lay, expect=e) for lay, e in [
+        ([_S357, [1, 10, 100], 0], True), ([_S357, [1, 3, 15], 0], True), ([_S357, [1, 3, -15], 1000], False),
+        ([_S357, [1, 21, 3], 0], False), ([_S357, [35, 7, 1], 0], False), ([_S357, [2, 6, 30], 0], False),
+        ([[], [], 0], True), ([[2, 0, 4], [1, 10, 100], 0], True), ([[2, 1, 4], [1, 1, 2], 0], True)]],
+    *[dict(src=f"{_LB}:782-806", op="flag", flag="c_prefer", layout=lay, expect=e) for lay, e in [
+        ([_S357, [100, 10, 1], 0], True), ([_S357, [35, 7, 1], 0], True), ([_S357, [-35, 7, 1], 1000], False),
+        ([_S357, [7, 21, 1], 0], False), ([_S357, [1, 3, 15], 0], False), ([_S357, [70, 14, 2], 0], False),
+        ([[], [], 0], True), ([[2, 0, 4], [1, 10, 100], 0], True), ([[2, 1, 4], [4, 1, 1], 0], True)]],
+    *[dict(src=f"{_LB}:809-825", op="flag", flag="f_contig", layout=lay, expect=e) for lay, e in [
+        ([_S357, [1, 3, 15], 0], True), ([_S357, [1, 4, 20], 0], False), ([[], [], 0], True),
+        ([[2, 0, 4], [1, 10, 100], 0], True), ([[2, 1, 4], [1, 1, 2], 0], True)]],
+    *[dict(src=f"{_LB}:828-844", op="flag", flag="c_contig", layout=lay, expect=e) for lay, e in [
+        ([_S357, [35, 7, 1], 0], True), ([_S357, [36, 7, 1], 0], False), ([[], [], 0], True),
+        ([[2, 0, 4], [1, 10, 100], 0], True), ([[2, 1, 4], [4, 1, 1], 0], True)]],
+    dict(src=f"{_LM}:563-570", op="matmul_layout", order="C", la=_c([4]), lb=_c([4]), expect=[[], [], 0]),
+    dict(src=f"{_LM}:572-575", op="matmul_layout", order="C", la=_c([5]), lb=_swap(_f([3, 4, 5, 6]), 0, 1),
+         expect=_c([4, 3, 6])),
+    dict(src=f"{_LM}:577-580", op="matmul_layout", order="C", la=_swap(_f([3, 4, 5, 6]), 0, 1), lb=_c([6]),
+         expect=_c([4, 3, 5])),
+    dict(src=f"{_LM}:582-585", op="matmul_layout", order="C", la=_c([7, 6]), lb=_swap(_f([2, 3, 4, 5, 6]), -1, -2),
+         expect=_c([2, 3, 4, 7, 5])),
+    dict(src=f"{_LM}:587-590", op="matmul_layout", order="C", la=_swap(_f([2, 3, 4, 5, 6]), -1, -2), lb=_c([5, 7]),
+         expect=_c([2, 3, 4, 6, 7])),
+    dict(src=f"{_LM}:592-595", op="matmul_layout", order="C", la=_swap(_f([4, 1, 2, 5, 6]), 0, 2),
+         lb=_swap(_f([4, 3, 1, 6, 7]), 0, 2), expect=_c([2, 3, 4, 5, 7])),
+    dict(src=f"{_LM}:597-600", op="matmul_layout", order="C", la=_swap(_f([4, 3, 2, 5, 6]), 0, 2),
+         lb=_swap(_f([4, 3, 2, 6, 7]), 0, 2), expect=_c([2, 3, 4, 5, 7])),
+    dict(src=f"{_LM}:602-607", op="matmul_layout", order="F", la=_f([5, 6]), lb=_f([6, 7]), expect=_f([5, 7])),
+    dict(src=f"{_LM}:609-613", op="matmul_layout", order="F", la=_f([5]), lb=_f([5, 6, 3, 4]), expect=_f([6, 3, 4])),
+    dict(src=f"{_LM}:615-619", op="matmul_layout", order="F", la=_f([5, 6, 3, 4]), lb=_f([6]), expect=_f([5, 3, 4])),
+    dict(src=f"{_LM}:621-626", op="matmul_layout", order="F", la=_f([5, 6, 2, 1, 4]), lb=_f([6, 7, 1, 3, 4]),
+         expect=_f([5, 7, 2, 3, 4])),
+    *[dict(src=f"{_BR}:{line}", op="broadcast", order="C", la=_c(a), lb=_c(b), expect_shape=e) for a, b, e, line in [
+        ([8, 1, 6, 1], [7, 1, 5], [8, 7, 6, 5], "287-294"), ([5, 4], [1], [5, 4], "299-306"),
+        ([5, 4], [4], [5, 4], "311-318"), ([15, 3, 5], [15, 1, 5], [15, 3, 5], "323-330"),
+        ([15, 3, 5], [3, 5], [15, 3, 5], "335-342"), ([15, 3, 5], [3, 1], [15, 3, 5], "347-354"),
+        ([1, 1, 2], [1, 2], [1, 1, 2], "357-364"), ([1, 2], [1, 1, 2], [1, 1, 2], "367-374"),
+        ([3], [4], None, "381-384"), ([2, 1], [8, 4, 3], None, "387-390"), ([15, 3, 5], [15, 3], None, "394-397")]],
+    dict(src=f"{_BR}:406-414", op="broadcast", order="C", la=_c([8, 1, 6, 3, 1]), lb=_f([7, 1, 3, 5]),
+         expect_shape=[8, 7, 6, 3, 5], expect_a=[18, 0, 3, 1, 0], expect_b=[0, 1, 0, 7, 21]),
+]
+
+
 def main() -> None:
     here = Path(__file__).resolve().parent
     out = here / "reference_kats.json"
@@ -426,6 +509,9 @@ def main() -> None:
     out = here / "creation_kats.json"
     out.write_text(json.dumps(CREATION_CASES, indent=1) + "\n")
     print(f"wrote {len(CREATION_CASES)} cases to {out}")
+    out = here / "layout_kats.json"
+    out.write_text(json.dumps(LAYOUT_CASES, indent=1) + "\n")
+    print(f"wrote {len(LAYOUT_CASES)} cases to {out}")
 
 
 if __name__ == "__main__":
