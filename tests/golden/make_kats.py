@@ -480,6 +480,15 @@ LAYOUT_CASES = [
         ([3], [4], None, "381-384"), ([2, 1], [8, 4, 3], None, "387-390"), ([15, 3, 5], [15, 3], None, "394-397")]],
     dict(src=f"{_BR}:406-414", op="broadcast", order="C", la=_c([8, 1, 6, 3, 1]), lb=_f([7, 1, 3, 5]),
          expect_shape=[8, 7, 6, 3, 5], expect_a=[18, 0, 3, 1, 0], expect_b=[0, 1, 0, 7, 21]),
+    # output shapes of `%` on contiguous operands (rstsr-core/src/device_faer/matmul.rs)
+    *[dict(src=f"rstsr-core/src/device_faer/matmul.rs:{line}", op="matmul_layout", order=o,
+           la=(_c if o == "C" else _f)(a), lb=(_c if o == "C" else _f)(b), expect_shape=e) for a, b, o, e, line in [
+        ([3], [2, 3, 5], "C", [2, 5], "264-268"), ([2, 3, 5], [5], "C", [2, 3], "270-274"),
+        ([5, 3], [2, 3, 5], "C", [2, 5, 5], "276-280"), ([2, 3, 5], [5, 3], "C", [2, 3, 3], "282-286"),
+        ([5, 3, 2], [3], "F", [5, 2], "293-297"), ([5], [5, 3, 2], "F", [3, 2], "299-303"),
+        ([5, 3, 2], [3, 5], "F", [5, 5, 2], "305-309"), ([3, 5], [5, 3, 2], "F", [3, 3, 2], "311-315"),
+        ([1, 3, 5], [2, 5, 3], "C", [2, 3, 3], "328-331"), ([2, 3, 5], [1, 5, 3], "C", [2, 3, 3], "337-340"),
+        ([1, 3, 5], [1, 5, 3], "C", [1, 3, 3], "347-350")]],
 ]
 
 
