@@ -95,7 +95,9 @@ typedef struct rstsr_ctx rstsr_ctx;
  * load's error. */
 int rstsr_cuda_ctx_create(int32_t device, rstsr_ctx** out);
 int rstsr_cuda_ctx_destroy(rstsr_ctx* ctx);
-/* Blocks until all work queued on the context's stream is done. */
+/* Blocks until all work queued on the context's stream is done. The
+ * reference's device calls are synchronous, so it has no counterpart; neither
+ * have the stream, launch-count and version queries below. */
 int rstsr_cuda_ctx_sync(rstsr_ctx* ctx);
 /* Replace the stream work is queued on (NULL restores the owned stream). */
 int rstsr_cuda_ctx_set_stream(rstsr_ctx* ctx, void* cuda_stream);
@@ -104,7 +106,8 @@ void* rstsr_cuda_ctx_get_stream(rstsr_ctx* ctx);
 int32_t rstsr_cuda_ctx_device(const rstsr_ctx* ctx);
 /* Number of kernels this library launched through the context so far. */
 uint64_t rstsr_cuda_ctx_launch_count(const rstsr_ctx* ctx);
-/* Message of the last failed call on this host thread ("" if none). */
+/* Message of the last failed call on this host thread ("" if none): the text of
+ * the rstsr_common::Error the status code stands for (rstsr-common/src/error.rs:15-48). */
 const char* rstsr_cuda_last_error(void);
 /* Library version string. */
 const char* rstsr_cuda_version(void);
@@ -235,7 +238,8 @@ int rstsr_cuda_binary(rstsr_ctx* ctx, rstsr_binary_op op, rstsr_dtype t,
                       const void* a, const rstsr_layout* la,
                       const void* b, const rstsr_layout* lb);
 
-/* op_mutc_refa_numb / op_mutc_numa_refb: one operand is a HOST scalar of type
+/* op_mutc_refa_numb / op_mutc_numa_refb (rstsr-core/src/operators/ops/
+ * op_ternary_arithmetic.rs:3-48): one operand is a HOST scalar of type
  * t. scalar_is_lhs = 0 computes c = a (op) s, 1 computes c = s (op) a. */
 int rstsr_cuda_binary_scalar(rstsr_ctx* ctx, rstsr_binary_op op, rstsr_dtype t,
                              void* c, const rstsr_layout* lc,
@@ -319,7 +323,8 @@ typedef enum {
 } rstsr_compare_op;
 int rstsr_cuda_compare(rstsr_ctx* ctx, rstsr_compare_op op, rstsr_dtype t, void* c, const rstsr_layout* lc,
                        const void* a, const rstsr_layout* la, const void* b, const rstsr_layout* lb);
-/* One operand a HOST scalar of type t (scalar_is_lhs as in rstsr_cuda_binary_scalar). */
+/* One operand a HOST scalar of type t (op_mutc_refa_numb / op_mutc_numa_refb of
+ * op_ternary_common.rs; scalar_is_lhs as in rstsr_cuda_binary_scalar). */
 int rstsr_cuda_compare_scalar(rstsr_ctx* ctx, rstsr_compare_op op, rstsr_dtype t, void* c,
                               const rstsr_layout* lc, const void* a, const rstsr_layout* la,
                               const void* scalar, int32_t scalar_is_lhs);
@@ -369,7 +374,8 @@ typedef enum {
 /* Output dtype of a reduction over input dtype ta (T, T::Real, bool or usize). */
 int rstsr_cuda_reduce_out_dtype(rstsr_reduce_op op, rstsr_dtype ta, rstsr_dtype* tout);
 
-/* Op*API::*_all: reduce every element; the scalar is written to HOST memory at
+/* Op*API::*_all (rstsr-core/src/operators/reduction.rs:3-33; rayon device
+ * feature_rayon/auto_impl/reduction.rs:7-716): reduce every element; the scalar is written to HOST memory at
  * out_host (one element of the output dtype). Synchronises. Zero-size input
  * is an InvalidValue error for min/max, as in the reference. */
 int rstsr_cuda_reduce_all(rstsr_ctx* ctx, rstsr_reduce_op op, rstsr_dtype ta,
@@ -390,7 +396,8 @@ int rstsr_cuda_reduce_axes(rstsr_ctx* ctx, rstsr_reduce_op op, rstsr_dtype ta,
                            const int64_t* axes, int32_t naxes,
                            void** out, rstsr_layout* lout);
 
-/* Same reduction into caller-provided storage: lout must have the kept-axes
+/* Same reduction into caller-provided storage (no reference counterpart: the
+ * reference's *_axes always allocate): lout must have the kept-axes
  * shape (any strides). */
 int rstsr_cuda_reduce_axes_into(rstsr_ctx* ctx, rstsr_reduce_op op, rstsr_dtype ta,
                                 const void* a, const rstsr_layout* la,
@@ -404,7 +411,8 @@ int rstsr_cuda_reduce_axes_into(rstsr_ctx* ctx, rstsr_reduce_op op, rstsr_dtype 
 int rstsr_cuda_argreduce_all(rstsr_ctx* ctx, int32_t is_max, rstsr_dtype ta,
                              const void* a, const rstsr_layout* la, uint64_t* out_host);
 
-/* arg*_axes: per kept element, the C-order index within the reduced-axes shape
+/* OpArgMaxAPI / OpArgMinAPI::arg*_axes (feature_rayon/auto_impl/reduction.rs:356-464,
+ * rstsr-native-impl/src/cpu_serial/reduction.rs:425-580): per kept element, the C-order index within the reduced-axes shape
  * (axes in the order given) of the first extreme element. Output dtype U64. */
 int rstsr_cuda_argreduce_axes(rstsr_ctx* ctx, int32_t is_max, rstsr_dtype ta,
                               const void* a, const rstsr_layout* la,
@@ -536,7 +544,8 @@ typedef struct {
 int rstsr_cuda_gemm_grouped(rstsr_ctx* ctx, rstsr_dtype t, const rstsr_gemm_problem* problems,
                             int32_t nproblems, const rstsr_gemm_opts* opts);
 
-/* Ozaki split statistics of the last f64 GEMM on this thread: slices used. */
+/* Ozaki split statistics of the last f64 GEMM on this thread: slices used (no
+ * reference counterpart). */
 int32_t rstsr_cuda_last_ozaki_slices(void);
 
 /* ------------------------------------------------------ contractions */
@@ -552,7 +561,8 @@ int32_t rstsr_cuda_last_ozaki_slices(void);
 int rstsr_cuda_einsum(rstsr_ctx* ctx, rstsr_dtype t, const char* subscripts, int32_t nops,
                       const void* const* ops, const rstsr_layout* lops, void* out,
                       const rstsr_layout* lout, const rstsr_gemm_opts* opts);
-/* Output extents of an einsum (host only). shape_out holds RSTSR_MAX_NDIM. */
+/* Output extents of an einsum (host only; the output labels and extents of
+ * crates-plugin/rstsr-tblis/src/einsum_impl.rs:146-199). shape_out holds RSTSR_MAX_NDIM. */
 int rstsr_cuda_einsum_output_shape(const char* subscripts, int32_t nops, const rstsr_layout* lops,
                                    int32_t* ndim_out, int64_t* shape_out);
 
@@ -601,7 +611,7 @@ int rstsr_cuda_trsm(rstsr_ctx* ctx, rstsr_order order, char side, char uplo, cha
 /* ---------------------------------------------------------------- graphs */
 
 /* Capture every call made on the context between begin and end into a CUDA
- * graph, then replay it with one launch. */
+ * graph, then replay it with one launch (no reference counterpart). */
 typedef struct rstsr_graph rstsr_graph;
 int rstsr_cuda_graph_begin(rstsr_ctx* ctx);
 int rstsr_cuda_graph_end(rstsr_ctx* ctx, rstsr_graph** out);
@@ -612,7 +622,8 @@ int rstsr_cuda_graph_destroy(rstsr_graph* g);
 
 /* Time the GEMM tile configurations for one problem shape and remember the
  * fastest for that (m, n, k, dtype, precision) class. The table can be saved
- * and loaded as text. */
+ * and loaded as text (no reference counterpart: rstsr's CPU GEMMs take their
+ * blocking from faer or the BLAS library). */
 int rstsr_cuda_autotune_gemm(rstsr_ctx* ctx, rstsr_dtype t, int64_t m, int64_t n, int64_t k,
                              const rstsr_gemm_opts* opts, int32_t* best_config);
 int rstsr_cuda_autotune_save(const char* path);
