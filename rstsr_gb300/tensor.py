@@ -534,7 +534,7 @@ def arange(start, stop=None, step=1, *, dtype=None, device: DeviceCuda) -> Tenso
     if stop is None:
         start, stop = 0, start
     if dtype is None:
-        dtype = np.float64 if any(isinstance(v, float) for v in (start, stop, step)) else np.int64
+        dtype = np.float64 if any(isinstance(v, (float, np.floating)) for v in (start, stop, step)) else np.int64
     code = dtype if isinstance(dtype, int) else dtype_code(dtype)
     s, e, st = (_scalar_bytes(v, code) for v in (start, stop, step))
     n = C.c_int64()
