@@ -25,6 +25,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import subprocess
 import sys
@@ -1049,10 +1050,11 @@ def wl_bytes(t):
 # ------------------------------------------------------------ CPU legs
 
 
-def cpu_sample_step(batch, nthreads, seed=0):
+def cpu_sample_step(batch, nthreads, seed=0, reps=1):
     """One bounded sample of the step on the CPU oracle (OpenMP restatement of
     the reference's rayon kernels): the first `batch` of the 32 leading
-    indices, all dtypes and layouts. Returns (seconds, algorithmic bytes)."""
+    indices, all dtypes and layouts, each case's operations timed `reps`
+    times. Returns (seconds, algorithmic bytes)."""
     from oracle import oracle as O
 
     shape = (batch,) + SHAPE[1:]
@@ -1067,26 +1069,26 @@ def cpu_sample_step(batch, nthreads, seed=0):
             b = O.Strided(host_data(dt, blen, seed + 1000 + 10 * di + li), shape, stride, off)
             cst = O.Strided(cbuf, shape, (0, CSHAPE[3], 0, 1), 0)
             pshape, pstride = permuted_view(shape, stride)
-            t0 = time.perf_counter()
-            if kind != "perm":
-                dst = O.empty_strided(pshape, c_stride(pshape), dt)
-                O.assign_arbitrary(dst, O.Strided(a.buf, pshape, pstride, off), 0, nthreads)
-            # the reference's two passes: tmp = a*b in the binary-op layout, tmp += c
-            from oracle import layout as OL
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                if kind != "perm":
+                    dst = O.empty_strided(pshape, c_stride(pshape), dt)
+                    O.assign_arbitrary(dst, O.Strided(a.buf, pshape, pstride, off), 0, nthreads)
+                # the reference's two passes: tmp = a*b in the binary-op layout, tmp += c
+                from oracle import layout as OL
 
-            lab = OL.layout_for_binary_op((shape, stride, off), (shape, stride, off))
-            tmp = O.empty_strided(lab[0], lab[1], dt)
-            O.binary("mul", tmp, a, b, nthreads)
-            O.binary("add", tmp, tmp, cst, nthreads)
-            osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [1, 3])
-            so = O.empty_strided(osh, ost, dt)
-            O.reduce_axes("sum", a, [1, 3], so, nthreads)
-            osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [3])
-            go = O.empty_strided(osh, ost, np.uint64)
-            O.argreduce_axes(True, a, [3], go, nthreads)
-            tot_t += time.perf_counter() - t0
-            nb = op_bytes_n(esize, kind, n, shape)
-            tot_b += nb
+                lab = OL.layout_for_binary_op((shape, stride, off), (shape, stride, off))
+                tmp = O.empty_strided(lab[0], lab[1], dt)
+                O.binary("mul", tmp, a, b, nthreads)
+                O.binary("add", tmp, tmp, cst, nthreads)
+                osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [1, 3])
+                so = O.empty_strided(osh, ost, dt)
+                O.reduce_axes("sum", a, [1, 3], so, nthreads)
+                osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [3])
+                go = O.empty_strided(osh, ost, np.uint64)
+                O.argreduce_axes(True, a, [3], go, nthreads)
+                tot_t += time.perf_counter() - t0
+                tot_b += op_bytes_n(esize, kind, n, shape)
     return tot_t, tot_b
 
 
@@ -1101,9 +1103,13 @@ def cpu_baseline(args):
 
     nth = O.max_threads()
     batch = args.cpu_batch
-    t, b = cpu_sample_step(batch, nth)
+    t, b = cpu_sample_step(batch, nth)  # one pass sizes the repeat count
+    reps = max(1, min(200, math.ceil(args.cpu_seconds / max(t, 1e-3))))
+    if reps > 1:
+        t, b = cpu_sample_step(batch, nth, reps=reps)
     return {"value": round(b / t / 1e9, 2), "unit": "GB/s", "cores": nth, "kind": "port",
-            "sample": f"one step at leading extent {batch} of 32 (all dtypes and layouts), {b / 1e9:.2f} GB in {t:.2f} s"}
+            "sample": f"the step at leading extent {batch} of 32 (all dtypes and layouts), each case's operations "
+                      f"timed {reps} times: {b / 1e9:.2f} GB in {t:.2f} s"}
 
 
 def run_reference(args):
@@ -1155,6 +1161,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-gemm", action="store_true")
     ap.add_argument("--cpu-batch", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="CPU work the cpu_baseline sample is sized to (the operations repeated)")
     # restrict the workload (profiling a small case): comma-separated subsets
     ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
