@@ -132,6 +132,12 @@ int rstsr_cuda_layout_greedy(const rstsr_layout* l, int32_t keep_shape, rstsr_la
 /* Contiguity flags of layoutbase.rs:89-205, bit 0 c_contig, 1 f_contig,
  * 2 c_prefer, 3 f_prefer. */
 int32_t rstsr_cuda_layout_flags(const rstsr_layout* l);
+/* unravel_index_c / unravel_index_f (rstsr-common/src/layout/shape.rs:62-69, tested
+ * at layoutbase.rs:988-996): the multi-index of flat position `index` in `shape`,
+ * last axis fastest (RSTSR_ROW_MAJOR) or first axis fastest. Turns the raveled
+ * indices of rstsr_cuda_argreduce_* into the OpUnraveledArgMaxAPI /
+ * OpUnraveledArgMinAPI results (operators/reduction.rs:35-70). */
+int rstsr_cuda_unravel_index(const int64_t* shape, int32_t ndim, uint64_t index, rstsr_order order, int64_t* out);
 
 /* ---------------------------------------------------------------- storage */
 

@@ -53,6 +53,9 @@ from .tensor import (  # noqa: F401
     to_contig,
     unary,
     unpack_tri,
+    unravel_index,
+    unraveled_argmax_all,
+    unraveled_argmin_all,
     vecdot,
     zeros,
 )

@@ -155,6 +155,7 @@ _SIGS = {
     "rstsr_cuda_layout_for_array_copy": ([_L, C.c_char, _L], C.c_int),
     "rstsr_cuda_layout_greedy": ([_L, _I, _L, C.POINTER(C.c_int32)], C.c_int),
     "rstsr_cuda_layout_flags": ([_L], C.c_int32),
+    "rstsr_cuda_unravel_index": ([C.POINTER(C.c_int64), _I, C.c_uint64, _I, C.POINTER(C.c_int64)], C.c_int),
     "rstsr_cuda_malloc": ([_P, C.c_size_t, C.POINTER(_P)], C.c_int),
     "rstsr_cuda_free": ([_P, _P], C.c_int),
     "rstsr_cuda_memcpy_h2d": ([_P, _P, _P, C.c_size_t], C.c_int),

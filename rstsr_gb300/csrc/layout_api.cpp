@@ -70,6 +70,26 @@ int rstsr_cuda_layout_greedy(const rstsr_layout* l, int32_t keep_shape, rstsr_la
     return RSTSR_OK;
 }
 
+int rstsr_cuda_unravel_index(const int64_t* shape, int32_t ndim, uint64_t index, rstsr_order order,
+                             int64_t* out) {
+    clear_error();
+    if (ndim < 0 || ndim > RSTSR_MAX_NDIM) return fail(RSTSR_ERR_INVALID_VALUE, "unravel_index: ndim outside [0, 8]");
+    if (ndim > 0 && (!shape || !out)) return fail(RSTSR_ERR_INVALID_VALUE, "unravel_index: null argument");
+    uint64_t size = 1;
+    for (int i = 0; i < ndim; ++i) {
+        if (shape[i] < 0) return fail(RSTSR_ERR_INVALID_VALUE, "unravel_index: negative extent");
+        size *= (uint64_t)shape[i];
+    }
+    if (index >= size) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "unravel_index: index outside the shape");
+    // C order: the last axis varies fastest; F order: the first
+    for (int k = 0; k < ndim; ++k) {
+        const int i = order == RSTSR_ROW_MAJOR ? ndim - 1 - k : k;
+        out[i] = (int64_t)(index % (uint64_t)shape[i]);
+        index /= (uint64_t)shape[i];
+    }
+    return RSTSR_OK;
+}
+
 int32_t rstsr_cuda_layout_flags(const rstsr_layout* l) {
     if (!l || l->ndim < 0 || l->ndim > RSTSR_MAX_NDIM) return -1;
     Layout L = Layout::from_abi(*l);

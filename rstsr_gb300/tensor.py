@@ -729,6 +729,26 @@ def reduce_axes(op: str, t: Tensor, axes) -> Tensor:
     return Tensor(st, lout.shape_t, lout.stride_t, lout.offset, tout.value)
 
 
+def unravel_index(shape, index: int, order="C") -> tuple:
+    """unravel_index_c / unravel_index_f (rstsr-common/src/layout/shape.rs:62-69)."""
+    shape = tuple(int(s) for s in shape)
+    sh = (C.c_int64 * max(len(shape), 1))(*shape)
+    out = (C.c_int64 * max(len(shape), 1))()
+    call("rstsr_cuda_unravel_index", sh, len(shape), int(index), _order_code(order), out)
+    return tuple(int(out[i]) for i in range(len(shape)))
+
+
+def unraveled_argmax_all(t: Tensor) -> tuple:
+    """OpUnraveledArgMaxAPI::unraveled_argmax_all: the multi-index of the first
+    maximum (C-order flat index unravelled over the shape)."""
+    return unravel_index(t.shape, argreduce_all(True, t), "C")
+
+
+def unraveled_argmin_all(t: Tensor) -> tuple:
+    """OpUnraveledArgMinAPI::unraveled_argmin_all."""
+    return unravel_index(t.shape, argreduce_all(False, t), "C")
+
+
 def argreduce_all(is_max: bool, t: Tensor) -> int:
     out = C.c_uint64()
     call(

@@ -161,3 +161,28 @@ def test_reduce_output_dtypes_follow_reference(built_lib):
     for op in ("min", "max", "prod", "mean"):
         assert out(op, BOOL) == ("err", 2), op
     assert out("sum", 99) == ("err", 2)
+
+
+def test_unravel_index_matches_reference_and_numpy(built_lib):
+    """unravel_index_c / unravel_index_f (rstsr-common/src/layout/layoutbase.rs:988-996:
+    shape [3, 2, 6], flat 16 -> [1, 0, 4] in C order, [1, 1, 2] in F order), then a
+    sweep against numpy.unravel_index; an index outside the shape is refused."""
+    import numpy as np
+
+    import rstsr_gb300 as rt
+
+    assert rt.unravel_index((3, 2, 6), 0, "C") == (0, 0, 0)
+    assert rt.unravel_index((3, 2, 6), 16, "C") == (1, 0, 4)
+    assert rt.unravel_index((3, 2, 6), 0, "F") == (0, 0, 0)
+    assert rt.unravel_index((3, 2, 6), 16, "F") == (1, 1, 2)
+    assert rt.unravel_index((), 0, "C") == ()
+    rng = random.Random(4)
+    for _ in range(300):
+        shape = tuple(rng.randint(1, 6) for _ in range(rng.randint(1, 5)))
+        idx = rng.randrange(int(np.prod(shape)))
+        for order in ("C", "F"):
+            want = tuple(int(v) for v in np.unravel_index(idx, shape, order=order))
+            assert rt.unravel_index(shape, idx, order) == want
+    with pytest.raises(rt.RstsrError) as err:
+        rt.unravel_index((3, 2), 6, "C")
+    assert err.value.kind == "ValueOutOfRange"
