@@ -162,3 +162,16 @@ def test_oracle_linspace_and_tri_edges():
     assert (OC.tri_mask(x, 0, False) == np.tril(x)).all() and (OC.tri_mask(x, 2, True) == np.triu(x, 2)).all()
     assert (OC.tri_mask(x, 10, True) == 0).all() and (OC.tri_mask(x, -10, False) == 0).all()
     assert math.isclose(float(OC.linspace(0.0, 1.0, 11, np.float64)[3]), 0.3)
+
+
+def test_oracle_tri_mask_matches_numpy():
+    """numpy's tril / triu mask the last two axes with the same k convention: an
+    independent check of the oracle's masks on random shapes and offsets."""
+    rng = np.random.default_rng(12)
+    for _ in range(300):
+        nd = int(rng.integers(2, 5))
+        shape = tuple(int(v) for v in rng.integers(0, 6, nd))
+        x = rng.integers(1, 9, shape)
+        k = int(rng.integers(-7, 8))
+        np.testing.assert_array_equal(OC.tri_mask(x, k, False), np.tril(x, k))
+        np.testing.assert_array_equal(OC.tri_mask(x, k, True), np.triu(x, k))
