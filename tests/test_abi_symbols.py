@@ -4,6 +4,8 @@ import ctypes as C
 import re
 from pathlib import Path
 
+import pytest
+
 ROOT = Path(__file__).resolve().parent.parent
 
 
@@ -52,3 +54,26 @@ def test_version_and_error_plumbing(built_lib):
 def test_null_context_is_an_error_not_a_crash(built_lib):
     rc = built_lib.rstsr_cuda_ctx_sync(None)
     assert rc != 0
+
+
+@pytest.mark.parametrize("lang,std", [("c", "c99"), ("c++", "c++17")])
+def test_header_is_plain_c_and_cxx(tmp_path, lang, std):
+    """include/rstsr_cuda.h is the boundary for any FFI: it compiles as strict
+    C99 and as C++17 without warnings (plain pointers, sizes and enums only)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include <string.h>\n#include "rstsr_cuda.h"\nint main(void) {\n'
+                   '    const char* (*version)(void) = rstsr_cuda_version;\n'
+                   '    rstsr_layout l;\n'
+                   '    memset(&l, 0, sizeof l);\n'
+                   '    (void)version;\n'
+                   '    return l.ndim;\n}\n')
+    flags = ["-std=" + std, "-Wall", "-Wextra", "-Werror"] + (["-pedantic"] if lang == "c" else ["-x", "c++"])
+    res = subprocess.run([cc, *flags, "-I", str(ROOT / "include"), "-c", str(src), "-o", str(tmp_path / "o.o")],
+                         capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
