@@ -184,27 +184,3 @@ def test_isclose_matches_reference_formula(dev, dtype):
     for rtol, atol, en in ((1e-5, 1e-8, False), (1e-3, 0.0, True), (0.0, 1.0, False)):
         got = rt.isclose(ta, tb, rtol, atol, en).to_numpy()
         np.testing.assert_array_equal(got, E.isclose(a, b, rtol, atol, en))
-
-
-@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32])
-def test_allclose_is_all_of_isclose(dev, dtype):
-    """allclose_all (auto_impl/reduction.rs:717-749) against all(oracle isclose),
-    with broadcasting, NaN handling and the zero-size error."""
-    rng = np.random.default_rng(9)
-    x = (rng.standard_normal((64, 33)) * 100).astype(dtype)
-    for y, rtol, atol in [(x, 1e-5, 1e-8), ((x * (1 + 1e-7)).astype(dtype), 1e-5, 1e-8),
-                          ((x * (1 + 1e-7)).astype(dtype), 1e-9, 0.0), ((x + 1).astype(dtype), 1e-5, 1e-8),
-                          ((x + 1).astype(dtype), 0.0, 1.0)]:
-        want = bool(E.isclose(x, y, rtol, atol).all())
-        assert rt.allclose(rt.asarray(x, dev), rt.asarray(y, dev), rtol, atol) is want
-    rows = np.broadcast_to(x[0], (5, 33)).copy()
-    assert rt.allclose(rt.asarray(rows, dev), rt.asarray(x[0], dev)) is True
-    if dtype != np.int32:
-        xn = x.copy()
-        xn[3, 4] = np.nan
-        tn = rt.asarray(xn, dev)
-        assert rt.allclose(tn, tn) is False
-        assert rt.allclose(tn, tn, equal_nan=True) is True
-    with pytest.raises(RstsrError) as err:
-        rt.allclose(rt.asarray(np.zeros((0, 3), dtype=dtype), dev), rt.asarray(np.zeros((0, 3), dtype=dtype), dev))
-    assert err.value.kind == "InvalidValue"

@@ -1,12 +1,17 @@
 """arange / linspace / tril / triu on the GPU: the reference's creation
 known-answer tests, and bit-exact agreement with the oracle
-(oracle/creation.py) on value sweeps, strided and batched layouts."""
+(oracle/creation.py) on value sweeps, strided and batched layouts; and
+allclose_all against all(oracle isclose). The module is collected after the
+element-wise, GEMM, reduction and indexing modules (pytest orders files by
+name), before the allocation-free module that must run last."""
 
 import numpy as np
 import pytest
 
 import rstsr_gb300 as rt
 from oracle import creation as OC
+from oracle import elementwise as E
+from rstsr_gb300._lib import RstsrError
 from tests.test_creation_oracle import CASES, DT, arange_args, check_values
 
 pytestmark = pytest.mark.gpu
@@ -120,3 +125,27 @@ def test_tri_mask_needs_two_axes(dev):
     with pytest.raises(rt.RstsrError) as err:
         rt.tril(rt.asarray(np.ones(4), dev))
     assert err.value.kind == "InvalidLayout"
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32])
+def test_allclose_is_all_of_isclose(dev, dtype):
+    """allclose_all (auto_impl/reduction.rs:717-749) against all(oracle isclose),
+    with broadcasting, NaN handling and the zero-size error."""
+    rng = np.random.default_rng(9)
+    x = (rng.standard_normal((64, 33)) * 100).astype(dtype)
+    for y, rtol, atol in [(x, 1e-5, 1e-8), ((x * (1 + 1e-7)).astype(dtype), 1e-5, 1e-8),
+                          ((x * (1 + 1e-7)).astype(dtype), 1e-9, 0.0), ((x + 1).astype(dtype), 1e-5, 1e-8),
+                          ((x + 1).astype(dtype), 0.0, 1.0)]:
+        want = bool(E.isclose(x, y, rtol, atol).all())
+        assert rt.allclose(rt.asarray(x, dev), rt.asarray(y, dev), rtol, atol) is want
+    rows = np.broadcast_to(x[0], (5, 33)).copy()
+    assert rt.allclose(rt.asarray(rows, dev), rt.asarray(x[0], dev)) is True
+    if dtype != np.int32:
+        xn = x.copy()
+        xn[3, 4] = np.nan
+        tn = rt.asarray(xn, dev)
+        assert rt.allclose(tn, tn) is False
+        assert rt.allclose(tn, tn, equal_nan=True) is True
+    with pytest.raises(RstsrError) as err:
+        rt.allclose(rt.asarray(np.zeros((0, 3), dtype=dtype), dev), rt.asarray(np.zeros((0, 3), dtype=dtype), dev))
+    assert err.value.kind == "InvalidValue"
