@@ -374,9 +374,13 @@ static int kt_for_stages(int slices, int bn) {
 // max over row mean |x|) of both operands. Dropping the levels >= L leaves an
 // error near 2^(-7L + spreadA + spreadB - 6) of the result (measured on GB300:
 // 2.5e-12 at L = 6 and 2.8e-13 at L = 7 for spreads 4.9 + 4.9); keeping it
-// below 2^-43 gives 7 L >= 37 + spreadA + spreadB.
-static int auto_levels(double spread_a, double spread_b) {
-    const double need = 37.0 + std::max(0.0, spread_a) + std::max(0.0, spread_b);
+// below 2^-43 gives 7 L >= 37 + spreadA + spreadB. Products whose results
+// cancel exceed that estimate (uniform(-1, 1) operands, K = 128: 2.0e-13 at
+// L = 6). Calls of at most 2^24 multiply-adds are bound by launch latency, not
+// by the tensor cores: they take one slice more (seven more bits, for
+// <= 1e-13 on such operands), which costs no time there.
+static int auto_levels(double spread_a, double spread_b, bool small) {
+    const double need = (small ? 44.0 : 37.0) + std::max(0.0, spread_a) + std::max(0.0, spread_b);
     int L = (int)std::ceil(need / 7.0);
     return std::min(std::max(L, 4), 8);
 }
@@ -508,7 +512,9 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
             float fa, fb;
             memcpy(&fa, &hsp[0], 4);
             memcpy(&fb, &hsp[1], 4);
-            L = auto_levels(fa, b_items.empty() ? fa : fb);
+            double macs = 0;
+            for (const auto& q : probs) macs += (double)q.M * (double)q.N * (double)q.K;
+            L = auto_levels(fa, b_items.empty() ? fa : fb, macs <= 16777216.0);
         }
         L = std::min(std::max(L, 1), 8);
     } else {
