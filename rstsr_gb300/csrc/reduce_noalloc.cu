@@ -42,28 +42,48 @@ static int scratch_address(int device, void** out) {
     return RSTSR_OK;
 }
 
+// The planner picks the number of chunks of the reduced range for
+// parallelism alone. When their partial sums do not fit the fixed scratch,
+// use as many chunks as fit (each chunk a multiple of the vector width, as the
+// planner keeps it), down to one unsplit pass that needs no scratch at all: a
+// large plan runs with fewer chunks instead of failing.
+template <typename T>
+static void fit_split_to_scratch(RedParams& p) {
+    using Acc = typename Red<T, kRedSum>::Acc;
+    if (p.nsplit <= 1) return;
+    const size_t per_split = (size_t)p.nout * sizeof(Acc);
+    if ((size_t)p.nsplit * per_split <= RSTSR_NOALLOC_SCRATCH_BYTES) return;
+    const int64_t fit = (int64_t)(RSTSR_NOALLOC_SCRATCH_BYTES / per_split);
+    if (fit < 2) {
+        p.nsplit = 1;
+        p.chunk = p.nred;
+        return;
+    }
+    constexpr int64_t VEC = 16 / sizeof(T) > 0 ? 16 / sizeof(T) : 1;
+    int64_t chunk = (p.nred + fit - 1) / fit;
+    chunk = (chunk + VEC - 1) / VEC * VEC;
+    p.chunk = chunk;
+    p.nsplit = (int32_t)((p.nred + chunk - 1) / chunk);
+}
+
 template <typename T>
 static int launch_sum_noalloc(cudaStream_t stream, RedParams p, void* scratch) {
     using Acc = typename Red<T, kRedSum>::Acc;
     const int64_t opc = red_outputs_per_cta(p);
     const int64_t gx = (p.nout + opc - 1) / opc;
     if (gx > INT32_MAX || p.nsplit > 65535) return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE, "reduction too large");
+    fit_split_to_scratch<T>(p);
     if (p.nsplit > 1) {
-        const size_t need = (size_t)p.nsplit * (size_t)p.nout * sizeof(Acc);
-        if (need > RSTSR_NOALLOC_SCRATCH_BYTES)
-            return fail(RSTSR_ERR_VALUE_OUT_OF_RANGE,
-                        "sum_axes_noalloc: this reduction needs " + std::to_string(need) +
-                            " bytes of scratch, more than the fixed " +
-                            std::to_string((size_t)RSTSR_NOALLOC_SCRATCH_BYTES) + " bytes");
         // every partial is written by the first kernel before the second
         // reads it, so the scratch needs no clearing
+        if ((size_t)p.nsplit * (size_t)p.nout * sizeof(Acc) > RSTSR_NOALLOC_SCRATCH_BYTES)
+            return fail(RSTSR_ERR_RUNTIME, "sum_axes_noalloc: split partials exceed the fixed scratch");
         p.partial = scratch;
     } else {
         p.partial = nullptr;
     }
-    reduce_kernel<T, kRedSum><<<dim3((unsigned)gx, (unsigned)p.nsplit), kRedThreads, 0, stream>>>(p);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "reduce_kernel");
+    cudaError_t e = launch_reduce_pass<T, kRedSum>(p, dim3((unsigned)gx, (unsigned)p.nsplit), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "reduce pass");
     if (p.nsplit > 1) {
         const int64_t gc = (p.nout + kRedThreads - 1) / kRedThreads;
         reduce_combine_kernel<T, kRedSum><<<(unsigned)gc, kRedThreads, 0, stream>>>(p);
@@ -89,6 +109,16 @@ extern "C" int rstsr_cuda_sum_axes_noalloc(void* stream, rstsr_dtype ta, const v
     if (naxes < 0 || (naxes > 0 && !axes)) return fail(RSTSR_ERR_INVALID_VALUE, "bad axes");
     int device = -1;
     RSTSR_CUDA_TRY(cudaGetDevice(&device));
+    {
+        // the scratch address and the SM count are those of the current
+        // device: a stream of another device is refused
+        int stream_device = -1;
+        RSTSR_CUDA_TRY(cudaStreamGetDevice((cudaStream_t)stream, &stream_device));
+        if (stream_device != device)
+            return fail(RSTSR_ERR_DEVICE_MISMATCH, "sum_axes_noalloc: the stream belongs to device " +
+                                              std::to_string(stream_device) + ", the current device is " +
+                                              std::to_string(device));
+    }
     void* scratch = nullptr;
     s = scratch_address(device, &scratch);
     if (s) return s;

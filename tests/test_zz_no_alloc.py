@@ -6,7 +6,9 @@ cannot take cudaMalloc's synchronisation, plugin hosts that forbid foreign
 allocations -- use this entry point: it takes a stream instead of a context
 and keeps its scratch in a fixed static device array. These tests call it
 through the C ABI and check it against the regular entry point,
-rstsr_cuda_reduce_axes_into, on two calls in a row. This file is collected
+rstsr_cuda_reduce_axes_into, and against the CPU oracle, on two calls in a
+row, in C and F layouts, including plans whose default split would need more
+than the fixed scratch. This file is collected
 last so that a failure here stops a -x run only after every other test.
 """
 
@@ -16,7 +18,9 @@ import numpy as np
 import pytest
 
 import rstsr_gb300 as rt
-from rstsr_gb300._lib import Layout, call, lib
+from oracle import layout as OL
+from oracle import oracle as O
+from rstsr_gb300._lib import call, lib
 
 pytestmark = pytest.mark.gpu
 
@@ -37,24 +41,51 @@ def noalloc_sum(dev, t, axes, out):
     assert rc == 0, lib().rstsr_cuda_last_error().decode()
 
 
+def oracle_sum(buf, shape, stride, axes, dtype):
+    """The oracle's sum; f32 inputs are summed in f64 (the oracle's own f32
+    sum of 2^19 elements carries about 1e-5 of rounding)."""
+    if dtype == np.float32:
+        buf, dtype = buf.astype(np.float64), np.float64
+    kept = [d for i, d in enumerate(shape) if i not in axes]
+    out = O.empty_strided(kept, OL.c_stride(kept), dtype)
+    O.reduce_axes("sum", O.Strided(buf, shape, stride, 0), list(axes), out, nthreads=O.max_threads())
+    return out.values()
+
+
+def check(got, want, dtype, what):
+    if np.dtype(dtype).kind == "f":
+        tol = F64_TOL if dtype == np.float64 else 1e-5
+        err = np.max(np.abs(got - want)) / max(np.max(np.abs(want)), 1e-300)
+        assert err <= tol, f"{what}: normwise rel err {err}"
+    else:
+        np.testing.assert_array_equal(got, want, err_msg=what)
+
+
 @pytest.mark.parametrize(
-    "shape,axes,dtype",
+    "shape,axes,dtype,order",
     [
-        ((4, 1 << 20), [1], np.float64),      # few outputs, long rows: split partials in the static scratch
-        ((1 << 18, 8), [0], np.float64),      # column regime with split partials
-        ((32, 64, 128, 128), [1, 3], np.float64),  # the workload's sum over axes (1, 3)
-        ((6, 1 << 19), [1], np.float32),
-        ((1 << 17, 5), [0], np.int32),
+        ((4, 1 << 20), [1], np.float64, "C"),      # few outputs, long rows: split partials in the static scratch
+        ((1 << 18, 8), [0], np.float64, "C"),      # column regime with split partials
+        ((32, 64, 128, 128), [1, 3], np.float64, "C"),  # the workload's sum over axes (1, 3)
+        ((32, 64, 128, 128), [1, 3], np.float32, "F"),  # the same on the F-ordered layout
+        ((6, 1 << 19), [1], np.float32, "C"),
+        ((1 << 17, 5), [0], np.int32, "C"),
+        # column regime whose default split needs more than the fixed scratch
+        # (about 4.9 MB of partials): it runs with fewer chunks instead
+        ((8192, 4096), [0], np.float64, "C"),
+        ((4096, 6000), [1], np.float32, "F"),       # F order, 4096 outputs along the contiguous axis
     ],
 )
-def test_noalloc_matches_regular_twice(dev, shape, axes, dtype):
+def test_noalloc_matches_regular_and_oracle_twice(dev, shape, axes, dtype, order):
     rng = np.random.default_rng(123)
+    stride = OL.c_stride(shape) if order == "C" else OL.f_stride(shape)
     for call_no in range(2):
+        n = int(np.prod(shape))
         if np.dtype(dtype).kind == "f":
-            x = rng.uniform(-1, 1, shape).astype(dtype)
+            buf = rng.uniform(-1, 1, n).astype(dtype)
         else:
-            x = rng.integers(-1000, 1001, shape).astype(dtype)
-        t = rt.asarray(x, dev)
+            buf = rng.integers(-1000, 1001, n).astype(dtype)
+        t = rt.from_host_layout(buf, shape, stride, 0, dev)
         kept = [d for i, d in enumerate(shape) if i not in axes]
         want = rt.empty(kept, dtype, dev)
         got = rt.empty(kept, dtype, dev)
@@ -62,13 +93,9 @@ def test_noalloc_matches_regular_twice(dev, shape, axes, dtype):
         regular_sum(dev, t, axes, want)
         noalloc_sum(dev, t, axes, got)
         dev.sync()
-        w, g = want.to_numpy(), got.to_numpy()
-        if np.dtype(dtype).kind == "f":
-            tol = F64_TOL if dtype == np.float64 else 1e-5
-            err = np.max(np.abs(g - w)) / max(np.max(np.abs(w)), 1e-300)
-            assert err <= tol, f"call {call_no}: normwise rel err {err}"
-        else:
-            np.testing.assert_array_equal(g, w)
+        g = got.to_numpy()
+        check(g, want.to_numpy(), dtype, f"call {call_no} vs the regular entry point")
+        check(g, oracle_sum(buf, shape, stride, axes, dtype), dtype, f"call {call_no} vs the oracle")
 
 
 def test_noalloc_rejects_unsupported_dtype(dev):
