@@ -153,6 +153,25 @@ int rstsr_cuda_memcpy_d2h(rstsr_ctx* ctx, void* dst, const void* src, size_t nby
 /* Stream-ordered, asynchronous copy between any two addresses the device can
  * reach (device memory or pinned host memory); does not synchronise. */
 int rstsr_cuda_memcpy_d2d(rstsr_ctx* ctx, void* dst, const void* src, size_t nbytes);
+/* DeviceChangeAPI host<->device moves for any host memory
+ * (rstsr-core/src/storage/conversion.rs:3-21; to_cpu_vec at storage/device.rs:33,
+ * from_cpu_vec / outof_cpu_vec at storage/creation.rs:11-13, which move an
+ * ordinary Vec<T> / &[T]).
+ * Page-locked host memory (cudaHostAlloc, cudaHostRegister): one
+ * stream-ordered copy; the call returns at once, the host buffer must stay
+ * valid and untouched until the stream reaches the copy (rstsr_cuda_ctx_sync
+ * or an event).
+ * Pageable host memory: chunks of 8 MiB through the context's ring of
+ * page-locked staging buffers (created by the first such call, freed with the
+ * context), the host copies overlapping the transfers.
+ *   h2d_async returns once every byte of src has been read: src may be reused
+ *   at once; the device side completes in stream order.
+ *   d2h_async returns once every byte has arrived in dst (it waits for the
+ *   work queued before it on the context's stream).
+ * A staged copy cannot be captured into a graph (RSTSR_ERR_RUNTIME). One
+ * staged copy runs at a time per context. */
+int rstsr_cuda_memcpy_h2d_async(rstsr_ctx* ctx, void* dst, const void* src, size_t nbytes);
+int rstsr_cuda_memcpy_d2h_async(rstsr_ctx* ctx, void* dst, const void* src, size_t nbytes);
 
 /* ------------------------------------------------------------- assignment */
 
@@ -438,13 +457,16 @@ int rstsr_cuda_argreduce_axes_into(rstsr_ctx* ctx, int32_t is_max, rstsr_dtype t
  * caller provides input and output, the output laid out over the kept axes
  * (any strides). The split reduction's partial sums live in one fixed static
  * device array of RSTSR_NOALLOC_SCRATCH_BYTES that every GPU loading this
- * library holds until the process exits; a reduction that would need more
- * scratch is rejected with RSTSR_ERR_VALUE_OUT_OF_RANGE. The first call on a
- * device looks up that array's device address (cudaGetSymbolAddress), so make
- * the first call on each device before any stream capture. All calls share
- * the array: calls that can overlap on the GPU (different streams, or
- * different host threads) race on it and must be serialised by the caller.
- * Supported dtypes: f64, f32, i32, i64. Never calls cudaMalloc or cudaFree. */
+ * library holds until the process exits; a reduction whose default split
+ * would need more scratch runs with fewer chunks of the reduced range (down
+ * to one unsplit pass, which needs none), so no valid input is rejected for
+ * its size. The stream must belong to the current device
+ * (RSTSR_ERR_DEVICE_MISMATCH otherwise). The first call on a device looks up
+ * that array's device address (cudaGetSymbolAddress), so make the first call
+ * on each device before any stream capture. All calls share the array: calls
+ * that can overlap on the GPU (different streams, or different host threads)
+ * race on it and must be serialised by the caller. Supported dtypes: f64,
+ * f32, i32, i64. Never calls cudaMalloc or cudaFree. */
 #define RSTSR_NOALLOC_SCRATCH_BYTES (1u << 20)
 int rstsr_cuda_sum_axes_noalloc(void* cuda_stream, rstsr_dtype ta, const void* a, const rstsr_layout* la,
                                 const int64_t* axes, int32_t naxes, void* out, const rstsr_layout* lout);

@@ -161,6 +161,8 @@ _SIGS = {
     "rstsr_cuda_memcpy_h2d": ([_P, _P, _P, C.c_size_t], C.c_int),
     "rstsr_cuda_memcpy_d2h": ([_P, _P, _P, C.c_size_t], C.c_int),
     "rstsr_cuda_memcpy_d2d": ([_P, _P, _P, C.c_size_t], C.c_int),
+    "rstsr_cuda_memcpy_h2d_async": ([_P, _P, _P, C.c_size_t], C.c_int),
+    "rstsr_cuda_memcpy_d2h_async": ([_P, _P, _P, C.c_size_t], C.c_int),
     "rstsr_cuda_assign": ([_P, _P, _L, _I, _P, _L, _I], C.c_int),
     "rstsr_cuda_assign_arbitrary": ([_P, _P, _L, _I, _P, _L, _I, _I], C.c_int),
     "rstsr_cuda_fill": ([_P, _P, _L, _I, _P], C.c_int),

@@ -9,11 +9,16 @@
 
 #include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "layout.hpp"
 #include "rstsr_cuda.h"
+
+namespace rstsr {
+struct StagingRing;  // page-locked buffers for pageable host transfers (transfer.cu)
+}
 
 struct rstsr_ctx {
     int device = 0;
@@ -25,6 +30,8 @@ struct rstsr_ctx {
     bool capturing = false;
     uint64_t launches_at_capture = 0;
     int* dev_err = nullptr;  // device word: non-zero after a kernel gave up a bounded wait
+    std::mutex staging_mu;
+    rstsr::StagingRing* staging = nullptr;  // created by the first pageable transfer
 };
 
 namespace rstsr {
@@ -40,6 +47,9 @@ int cuda_fail(cudaError_t e, const char* what);
 
 // After a launch: count it and surface launch-configuration errors.
 int after_launch(rstsr_ctx* ctx, const char* name);
+
+// Release the context's staging ring (transfer.cu); no-op without one.
+void staging_destroy(rstsr_ctx* ctx);
 
 // Validate a context pointer and make its device current.
 int enter(rstsr_ctx* ctx);

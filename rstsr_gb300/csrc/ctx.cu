@@ -197,6 +197,7 @@ int rstsr_cuda_ctx_destroy(rstsr_ctx* ctx) {
     if (!ctx) return RSTSR_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    staging_destroy(ctx);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     if (ctx->dev_err) cudaFree(ctx->dev_err);
     delete ctx;
