@@ -176,6 +176,17 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
     if (p.nred >= (int64_t(1) << 32) || p.nout >= (int64_t(1) << 32))
         return fail(RSTSR_ERR_UNIMPLEMENTED, "reductions over 2^32 or more elements per output");
     build_red_space(ls, &p.r);
+    // the flattened reduced index is the logical (C-order) index: every walk
+    // in index order visits the logical indices in increasing order
+    {
+        int64_t acc = 1;
+        bool mono = true;
+        for (int i = 0; i < p.r.nd; ++i) {
+            mono = mono && (p.r.shape[i] == 1 || p.r.lstride[i] == acc);
+            acc *= p.r.shape[i];
+        }
+        p.mono = mono ? 1 : 0;
+    }
     // kept space: operand 0 = input (drives the order), operand 1 = output
     {
         Layout lmi = lm, loo = Lo;
@@ -208,20 +219,25 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         p.nsplit = 1;
         p.chunk = 1;
     } else if (rin <= kin) {
-        // row regime
-        // group size: about four vector loads per lane for short runs, one
-        // CTA per output for long ones
-        int G = 256, glog = 8;
-        if (p.nred <= 4096) {
-            const int64_t want = (p.nred + (int64_t)VEC * 4 - 1) / ((int64_t)VEC * 4);
-            G = 1;
-            glog = 0;
-            while (G < want && G < 32) {
-                G <<= 1;
-                ++glog;
-            }
+        // row regime. Group size from the vector loads per output (nvec):
+        // short runs give each lane about 8 of them (one round of loads in
+        // flight; a warp's accesses stay whole 64-128-byte pieces of each
+        // run), long runs about 32 (four rounds: a CTA that issues only one
+        // round spends most of its life waiting for it); G <= 256
+        const int64_t W = p.r.stride[0] == 1 && (p.r.shape[0] % VEC) == 0 ? VEC : 1;
+        const int64_t nvec = (p.nred + W - 1) / W;
+        const int64_t per_lane = nvec <= 1024 ? 8 : 32;
+        int G = 1, glog = 0;
+        while (G < 256 && (int64_t)G * 2 * per_lane <= nvec) {
+            G <<= 1;
+            ++glog;
+        }
+        if (nvec <= 1024 && G > 32) {
+            G = 32;
+            glog = 5;
         }
         p.glog = glog;
+        p.row = 1;
         const int64_t gx = (p.nout + (kRedThreads / G) - 1) / (kRedThreads / G);
         int64_t nsplit = 1;
         if (gx < target && p.nred > (int64_t)G * VEC * 8)
@@ -239,6 +255,10 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         for (int i = 1; vec && i < p.r.nd; ++i) vec = (std::llabs(p.r.stride[i]) * (int64_t)es) % vb == 0;
         for (int i = 0; vec && i < p.k.nd; ++i) vec = (std::llabs(p.k.in_stride[i]) * (int64_t)es) % vb == 0;
         p.vec = vec ? 1 : 0;
+        // the group's step over the reduced elements as (rows, columns) of dim 0
+        const uint32_t step = (uint32_t)G * (uint32_t)(vec ? VEC : 1);
+        p.adv_row = step / p.r.shape[0];
+        p.adv_c = step % p.r.shape[0];
     } else {
         // column regime: a warp reads 32 neighbouring outputs' elements per
         // step. When kept dim 0 is contiguous in the input (and everything is
@@ -246,8 +266,9 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         // OV-wide vector load per reduced element; measured on GB300 the
         // scalar form reached 22 % of DRAM bandwidth (f32 sum_axes over an
         // F-ordered tensor, 4096 outputs), latency-bound with ~20 KB in
-        // flight per SM. Enough CTAs must be resident to keep ~40 KB per SM
-        // in flight: aim for two waves of 4 CTAs per SM.
+        // flight per SM. A CTA keeps 256 x 4 loads in flight (16 KB with
+        // 16-byte loads): aim for four CTAs per SM, each walking a long
+        // chunk (fewer partials to write and fold).
         p.glog = 0;
         const int OV = es >= 16 ? 1 : (16 / (int)es >= 4 ? 4 : 16 / (int)es);
         bool cv = OV > 1 && p.k.nd > 0 && p.k.in_stride[0] == 1 && (p.k.shape[0] % OV) == 0;
@@ -258,7 +279,7 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         p.ocol = cv ? OV : 1;
         const int64_t opc = (int64_t)kRedThreads * p.ocol;
         const int64_t gx = (p.nout + opc - 1) / opc;
-        const int64_t col_target = 8 * (int64_t)ctx->num_sms;
+        const int64_t col_target = 4 * (int64_t)ctx->num_sms;
         int64_t nsplit = 1;
         if (gx < col_target && p.nred > 16)
             nsplit = std::min<int64_t>((col_target + gx - 1) / gx, (p.nred + 15) / 16);

@@ -4,13 +4,14 @@
 //
 //   * the reduced axes and the kept axes are each collapsed into a small
 //     iteration space (inner-first, contiguous neighbours merged);
-//   * a group of G threads (G = 1, 32 or 256) owns one output element and
-//     strides over that element's reduced elements: G = 32/256 ("row" regime,
-//     reduced axes innermost in memory) reads each output's run with 16-byte
-//     vector loads and combines the group with warp shuffles and shared
-//     memory; G = 1 ("column" regime, a kept axis innermost) lets neighbouring
-//     threads own neighbouring outputs so every load is coalesced across the
-//     warp;
+//   * "row" regime (reduced axes innermost in memory, reduce_row_kernel): a
+//     group of G threads (G = 1 ... 256) owns one output element and walks its
+//     reduced elements with 16-byte vector loads, combining the group with
+//     warp shuffles and shared memory; "column" regime (a kept axis
+//     innermost, reduce_col_kernel): neighbouring threads own neighbouring
+//     outputs (several per thread with vector loads) so every load is
+//     coalesced across the warp; both walks advance a (row, column) position
+//     instead of decomposing every index;
 //   * when there are too few outputs to fill the 152 SMs, the reduced range
 //     is split into chunks over blockIdx.y; each chunk writes its accumulator
 //     to scratch and a second kernel folds the chunks in chunk order.
@@ -73,6 +74,12 @@ struct RedParams {
     int32_t op;      // rstsr_reduce_op (finalisation)
     int32_t ocol;    // column regime with vector loads: outputs per thread (1 = scalar)
     int64_t chunk;   // reduced elements per chunk
+    // row regime: a group step of G * W reduced elements (W = the vector
+    // width, or 1) moves the (row, column) position by adv_row rows and
+    // adv_c columns of reduced dim 0 (step = adv_row * shape[0] + adv_c)
+    uint32_t adv_row, adv_c;
+    int32_t row;   // row regime (G threads per output, G may be 1)
+    int32_t mono;  // the flattened reduced index is the logical index (walks visit it in order)
     void* partial;   // [nsplit][nout] accumulators, or null
     const void* in;
     void* out;
@@ -259,19 +266,46 @@ struct Red<T, kRedAny> {
     __device__ static Out fin(const Acc& s, int, int64_t) { return (uint8_t)s.a; }
 };
 
+// Every policy folds into a thread-local accumulator `Local` first, with the
+// element's logical index within the reduced set as a 32-bit value (the
+// planner refuses 2^32 or more reduced elements per output), and turns it
+// into its `Acc` for the shuffles, the partials and the finalisation. For the
+// value reductions Local is Acc.
+template <typename T, int KIND>
+struct RedLocal : Red<T, KIND> {
+    using R = Red<T, KIND>;
+    using Local = typename R::Acc;
+    __device__ static Local linit() { return R::init(); }
+    __device__ static void lfold(Local& s, T x, uint32_t li) { R::fold(s, x, (int64_t)li); }
+    __device__ static typename R::Acc to_acc(const Local& s) { return s; }
+    static constexpr bool kArg = false;
+    // (the ordered-walk key interface of the arg reductions; unused here)
+    using Key = int;
+    __device__ static Key kstart() { return 0; }
+    __device__ static Key key(T) { return 0; }
+    __device__ static Key kbest(Key a, Key) { return a; }
+    __device__ static bool kwins(Key, Key) { return false; }
+};
+
 // arg reductions: the smallest logical index among the extreme values; NaN is
 // never accepted, except that a NaN at logical index 0 makes the answer 0 (the
 // serial fold of cpu_serial/reduction.rs:425-477 starts from that element and
 // no comparison against NaN succeeds afterwards).
 //
 // The empty accumulator holds the worst value (-inf / the type's minimum for
-// argmax) at index INT64_MAX, so "strictly better, or equal at a smaller
-// index" covers it without a separate test, and the fold selects without
-// branches (the comparison-and-select chain bounded the argmax kernels).
+// argmax) at index "none", so "strictly better, or equal at a smaller index"
+// covers it without a separate test, and the fold selects without branches.
+// A floating-point NaN fails both comparisons and is never taken; the element
+// at logical index 0 is tested for NaN once per output, outside the loop.
 template <typename T, bool IS_MAX>
 struct RedArg {
     using Acc = AccArg<T>;
     using Out = uint64_t;
+    struct Local {
+        T v;
+        uint32_t idx;  // UINT32_MAX: empty
+    };
+    static constexpr bool kArg = true;
     __device__ static T start() {
         if constexpr (std::is_floating_point<T>::value) {
             return IS_MAX ? -(T)INFINITY : (T)INFINITY;
@@ -283,17 +317,29 @@ struct RedArg {
         }
     }
     __device__ static Acc init() { return {start(), INT64_MAX, 0}; }
-    __device__ static bool better(T x, int64_t ix, T v, int64_t iv) {
+    __device__ static Local linit() { return {start(), UINT32_MAX}; }
+    template <typename I>
+    __device__ static bool better(T x, I ix, T v, I iv) {
         return (IS_MAX ? (x > v) : (x < v)) | ((x == v) & (ix < iv));
     }
-    __device__ static void fold(Acc& s, T x, int64_t lidx) {
-        if (is_nan_v(x)) {
-            if (lidx == 0) s.nan0 = 1;
-            return;
-        }
-        const bool take = better(x, lidx, s.v, s.idx);
+    // Ordered walks (logical indices visited in increasing order): compare
+    // keys; a later equal key never wins, NaN never wins (its key fails every
+    // comparison, and fmax / fmin drop it).
+    using Key = T;
+    __device__ static Key kstart() { return start(); }
+    __device__ static Key key(T x) { return x; }
+    __device__ static Key kbest(Key a, Key b) {
+        if constexpr (std::is_floating_point<T>::value) return IS_MAX ? fmax(a, b) : fmin(a, b);
+        else return IS_MAX ? (a > b ? a : b) : (a < b ? a : b);
+    }
+    __device__ static bool kwins(Key a, Key b) { return IS_MAX ? (a > b) : (a < b); }
+    __device__ static void lfold(Local& s, T x, uint32_t li) {
+        const bool take = better(x, li, s.v, s.idx);
         s.v = take ? x : s.v;
-        s.idx = take ? lidx : s.idx;
+        s.idx = take ? li : s.idx;
+    }
+    __device__ static Acc to_acc(const Local& s) {
+        return {s.v, s.idx == UINT32_MAX ? INT64_MAX : (int64_t)s.idx, 0};
     }
     __device__ static void merge(Acc& s, const Acc& o) {
         s.nan0 |= o.nan0;
@@ -312,27 +358,46 @@ struct RedArg {
 // comparison per element made the f64 argmax FP64-bound. key(x) maps -0.0 to
 // +0.0 (they compare equal) and flips the magnitude bits of negatives, so
 // x < y  <=>  key(x) < key(y) and x == y <=> key(x) == key(y) for non-NaN x, y;
-// NaN is recognised from its bits. Same results as RedArg<double>.
+// NaN is recognised from its bits and skipped. Same results as RedArg<double>.
 template <bool IS_MAX>
 struct RedArgF64 {
     using Acc = AccArg<int64_t>;
     using Out = uint64_t;
+    struct Local {
+        int64_t v;
+        uint32_t idx;
+    };
+    static constexpr bool kArg = true;
     // keys of non-NaN doubles lie strictly inside (INT64_MIN, INT64_MAX)
     __device__ static Acc init() { return {IS_MAX ? INT64_MIN : INT64_MAX, INT64_MAX, 0}; }
-    __device__ static bool better(int64_t x, int64_t ix, int64_t v, int64_t iv) {
+    __device__ static Local linit() { return {IS_MAX ? INT64_MIN : INT64_MAX, UINT32_MAX}; }
+    template <typename I>
+    __device__ static bool better(int64_t x, I ix, int64_t v, I iv) {
         return (IS_MAX ? (x > v) : (x < v)) | ((x == v) & (ix < iv));
     }
-    __device__ static void fold(Acc& s, double xd, int64_t lidx) {
+    // ordered walks: the key of a NaN is the start value, which never wins
+    using Key = int64_t;
+    __device__ static Key kstart() { return IS_MAX ? INT64_MIN : INT64_MAX; }
+    __device__ static Key key(double xd) {
         int64_t b = __double_as_longlong(xd);
-        if ((b & INT64_MAX) > 0x7FF0000000000000LL) {  // NaN
-            if (lidx == 0) s.nan0 = 1;
-            return;
-        }
+        const bool nan = (b & INT64_MAX) > 0x7FF0000000000000LL;
+        if (b == INT64_MIN) b = 0;  // -0.0 -> +0.0
+        const int64_t k = b >= 0 ? b : (b ^ INT64_MAX);
+        return nan ? (IS_MAX ? INT64_MIN : INT64_MAX) : k;
+    }
+    __device__ static Key kbest(Key a, Key b) { return IS_MAX ? (a > b ? a : b) : (a < b ? a : b); }
+    __device__ static bool kwins(Key a, Key b) { return IS_MAX ? (a > b) : (a < b); }
+    __device__ static void lfold(Local& s, double xd, uint32_t li) {
+        int64_t b = __double_as_longlong(xd);
+        const bool nan = (b & INT64_MAX) > 0x7FF0000000000000LL;
         if (b == INT64_MIN) b = 0;  // -0.0 -> +0.0
         const int64_t key = b >= 0 ? b : (b ^ INT64_MAX);
-        const bool take = better(key, lidx, s.v, s.idx);
+        const bool take = !nan & better(key, li, s.v, s.idx);
         s.v = take ? key : s.v;
-        s.idx = take ? lidx : s.idx;
+        s.idx = take ? li : s.idx;
+    }
+    __device__ static Acc to_acc(const Local& s) {
+        return {s.v, s.idx == UINT32_MAX ? INT64_MAX : (int64_t)s.idx, 0};
     }
     __device__ static void merge(Acc& s, const Acc& o) {
         s.nan0 |= o.nan0;
@@ -356,6 +421,11 @@ struct Red<double, kRedArgMax> : RedArgF64<true> {};
 template <>
 struct Red<double, kRedArgMin> : RedArgF64<false> {};
 
+template <typename T>
+struct RedLocal<T, kRedArgMax> : Red<T, kRedArgMax> {};
+template <typename T>
+struct RedLocal<T, kRedArgMin> : Red<T, kRedArgMin> {};
+
 // ---------------------------------------------------------------- shuffles
 
 // Shuffle within segments of `width` lanes (a power of two <= 32).
@@ -370,8 +440,10 @@ __device__ __forceinline__ A shfl_down_acc(const A& a, int delta, int width) {
     return r;
 }
 
-// loads in flight per thread in the reduction loops
-constexpr int kRedUnroll = 4;
+// loads in flight per thread in the row walk and in the column walk (whose
+// OV-wide loads and OV accumulators take more registers)
+constexpr int kRedUnroll = 8;
+constexpr int kRedUnrollCol = 4;
 
 // ---------------------------------------------------------------- kernels
 
@@ -380,18 +452,34 @@ struct alignas(sizeof(T) * VEC) RVec {
     T v[VEC];
 };
 
-__device__ __forceinline__ int64_t red_offset(const RedSpace& r, uint32_t e, int64_t* lidx) {
-    int64_t off = 0, li = 0;
-    for (int i = 0; i < r.nd - 1; ++i) {
-        uint32_t q = r.div[i].div(e);
-        int64_t idx = (int64_t)(e - q * r.shape[i]);
-        off += idx * r.stride[i];
-        li += idx * r.lstride[i];
+// Input offset and logical index of row `row` of the reduced space: its dims
+// 1 .. nd-1 (dim 1 fastest); dim 0 is the column inside the row.
+__device__ __forceinline__ int64_t red_row_offset(const RedSpace& r, uint32_t row, uint32_t* lrow) {
+    int64_t off = 0;
+    uint32_t li = 0;
+    for (int i = 1; i < r.nd - 1; ++i) {
+        const uint32_t q = r.div[i].div(row);
+        const uint32_t idx = row - q * r.shape[i];
+        off += (int64_t)idx * r.stride[i];
+        li += idx * (uint32_t)r.lstride[i];
+        row = q;
+    }
+    if (r.nd > 1) {
+        off += (int64_t)row * r.stride[r.nd - 1];
+        li += row * (uint32_t)r.lstride[r.nd - 1];
+    }
+    *lrow = li;
+    return off;
+}
+
+__device__ __forceinline__ int64_t kept_offset(const KeptSpace& k, uint32_t e, bool out) {
+    int64_t off = 0;
+    for (int i = 0; i < k.nd - 1; ++i) {
+        const uint32_t q = k.div[i].div(e);
+        off += (int64_t)(e - q * k.shape[i]) * (out ? k.out_stride[i] : k.in_stride[i]);
         e = q;
     }
-    off += (int64_t)e * r.stride[r.nd - 1];
-    li += (int64_t)e * r.lstride[r.nd - 1];
-    *lidx = li;
+    if (k.nd > 0) off += (int64_t)e * (out ? k.out_stride[k.nd - 1] : k.in_stride[k.nd - 1]);
     return off;
 }
 
@@ -402,179 +490,269 @@ constexpr int red_col_vec() {
     return 16 / sizeof(T) >= 4 ? 4 : (16 / sizeof(T) >= 2 ? 2 : 1);
 }
 
-// Column regime with vector loads (p.ocol = red_col_vec<T>()): the innermost
-// kept dim is contiguous in the input, so OV neighbouring outputs read one
-// OV-wide vector per reduced element; a warp reads 32 * OV * sizeof(T) bytes
-// per step instead of 32 * sizeof(T), with OV accumulators per thread.
-template <typename T, int KIND>
-__device__ __forceinline__ void reduce_colvec(const RedParams& p) {
-    using R = Red<T, KIND>;
-    using Acc = typename R::Acc;
-    constexpr int OV = red_col_vec<T>();
-    const int64_t o0 = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * OV;
-    if (o0 >= p.nout) return;  // nout is a multiple of OV
-    const T* __restrict__ in = reinterpret_cast<const T*>(p.in);
-    int64_t base = p.in_off;
-    {
-        uint32_t e = (uint32_t)o0;
-        for (int i = 0; i < p.k.nd - 1; ++i) {
-            uint32_t q = p.k.div[i].div(e);
-            base += (int64_t)(e - q * p.k.shape[i]) * p.k.in_stride[i];
-            e = q;
-        }
-        if (p.k.nd > 0) base += (int64_t)e * p.k.in_stride[p.k.nd - 1];
-    }
-    Acc acc[OV];
-#pragma unroll
-    for (int j = 0; j < OV; ++j) acc[j] = R::init();
-    const int64_t rb = (int64_t)blockIdx.y * p.chunk;
-    const int64_t re = min(p.nred, rb + p.chunk);
-    for (int64_t r0 = rb; r0 < re; r0 += kRedUnroll) {
-        RVec<T, OV> v[kRedUnroll];
-        int64_t li[kRedUnroll];
-#pragma unroll
-        for (int u = 0; u < kRedUnroll; ++u)
-            if (r0 + u < re) {
-                const int64_t off = red_offset(p.r, (uint32_t)(r0 + u), &li[u]);
-                v[u] = *reinterpret_cast<const RVec<T, OV>*>(in + base + off);
-            }
-#pragma unroll
-        for (int u = 0; u < kRedUnroll; ++u)
-            if (r0 + u < re) {
-#pragma unroll
-                for (int j = 0; j < OV; ++j) R::fold(acc[j], v[u].v[j], li[u]);
-            }
-    }
-    if (p.partial) {
-        Acc* part = reinterpret_cast<Acc*>(p.partial) + (int64_t)blockIdx.y * p.nout + o0;
-#pragma unroll
-        for (int j = 0; j < OV; ++j) part[j] = acc[j];
-        return;
-    }
-    int64_t oo = p.out_off;
-    {
-        uint32_t e = (uint32_t)o0;
-        for (int i = 0; i < p.k.nd - 1; ++i) {
-            uint32_t q = p.k.div[i].div(e);
-            oo += (int64_t)(e - q * p.k.shape[i]) * p.k.out_stride[i];
-            e = q;
-        }
-        if (p.k.nd > 0) oo += (int64_t)e * p.k.out_stride[p.k.nd - 1];
-    }
-    // the OV outputs are neighbours along kept dim 0
-#pragma unroll
-    for (int j = 0; j < OV; ++j)
-        reinterpret_cast<typename R::Out*>(p.out)[oo + j * p.k.out_stride[0]] = R::fin(acc[j], p.op, p.nred);
-}
-
 // Outputs handled by one CTA.
 __host__ __device__ inline int64_t red_outputs_per_cta(const RedParams& p) {
     return (int64_t)(kRedThreads >> p.glog) * (p.ocol > 1 ? p.ocol : 1);
 }
 
+// Row regime: a group of G = 2^glog threads owns one output and walks its
+// reduced elements W at a time (W = VEC with p.vec: one vector load of
+// neighbours along the contiguous reduced dim 0; else 1). Lane l starts at
+// flattened reduced index rb + l W and steps by G W; its (row, column)
+// position advances by the host-computed (adv_row, adv_c), so a step costs an
+// add and a compare, plus the row's offset (one multiply for a 2-dim reduced
+// space, a division chain beyond), instead of a full index decomposition.
+template <typename T, int KIND, int W, bool MONO>
+__device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedParams& p, const T* __restrict__ in,
+                                                                   int64_t base, int lane, int G) {
+    using R = RedLocal<T, KIND>;
+    typename R::Local acc = R::linit();
+    const int64_t rb = (int64_t)blockIdx.y * p.chunk;
+    const int64_t re = min(p.nred, rb + p.chunk);
+    int64_t r = rb + (int64_t)lane * W;
+    if (r >= re) return acc;
+    const uint32_t n0 = p.r.shape[0];
+    const int64_t s0 = p.r.stride[0];
+    const uint32_t l0 = (uint32_t)p.r.lstride[0];
+    uint32_t row = p.r.div[0].div((uint32_t)r);
+    uint32_t c = (uint32_t)r - row * n0;
+    const int64_t step = (int64_t)G * W;
+    // ordered arg reductions with vector loads: the best key of each vector
+    // first, its position inside the vector located once at the end
+    constexpr bool kFast = R::kArg && MONO && W > 1;
+    [[maybe_unused]] typename R::Key best{};
+    [[maybe_unused]] uint32_t best_r = UINT32_MAX;
+    if constexpr (kFast) best = R::kstart();
+    // logical indices of the loads are kept only where they cannot be
+    // recomputed from the iteration's first flattened index (an arg reduction
+    // over a reduced space whose flattened and logical orders differ)
+    constexpr bool kKeepLi = R::kArg && !MONO;
+    for (; r < re;) {
+        const int64_t r0 = r;
+        RVec<T, W> v[kRedUnroll];
+        [[maybe_unused]] uint32_t li[kKeepLi ? kRedUnroll : 1];
+#pragma unroll
+        for (int u = 0; u < kRedUnroll; ++u) {
+            if (r0 + u * step < re) {
+                uint32_t lrow;
+                const int64_t off = red_row_offset(p.r, row, &lrow) + (int64_t)c * s0;
+                if constexpr (kKeepLi) li[u] = lrow + c * l0;
+                v[u] = *reinterpret_cast<const RVec<T, W>*>(in + base + off);
+            }
+            c += p.adv_c;
+            row += p.adv_row;
+            if (c >= n0) {
+                c -= n0;
+                ++row;
+            }
+        }
+        r = r0 + kRedUnroll * step;
+#pragma unroll
+        for (int u = 0; u < kRedUnroll; ++u)
+            if (r0 + u * step < re) {
+                const uint32_t lu = kKeepLi ? li[kKeepLi ? u : 0] : (uint32_t)(r0 + u * step);
+                if constexpr (kFast) {
+                    typename R::Key m = R::key(v[u].v[0]);
+#pragma unroll
+                    for (int j = 1; j < W; ++j) m = R::kbest(m, R::key(v[u].v[j]));
+                    const bool take = R::kwins(m, best);
+                    best = take ? m : best;
+                    best_r = take ? lu : best_r;
+                } else {
+#pragma unroll
+                    for (int j = 0; j < W; ++j) R::lfold(acc, v[u].v[j], lu + (uint32_t)j * l0);
+                }
+            }
+    }
+    if constexpr (kFast) {
+        if (best_r != UINT32_MAX) {
+            // the first element of the winning vector that holds the best key
+            // (best_r is its flattened index: a multiple of W inside a row)
+            const uint32_t brow = p.r.div[0].div(best_r);
+            uint32_t lrow;
+            const int64_t boff = red_row_offset(p.r, brow, &lrow) + (int64_t)(best_r - brow * n0) * s0;
+            const RVec<T, W> w = *reinterpret_cast<const RVec<T, W>*>(in + base + boff);
+            int jj = W - 1;
+#pragma unroll
+            for (int j = W - 1; j >= 0; --j) jj = R::key(w.v[j]) == best ? j : jj;
+            acc.v = best;
+            acc.idx = best_r + (uint32_t)jj;
+        }
+    }
+    return acc;
+}
+
+// Column regime: one thread owns OV neighbouring outputs (OV > 1: the kept
+// dim 0 is contiguous and one OV-wide vector load per reduced element serves
+// them all) and walks the reduced elements of its chunk in order, the
+// (row, column) position advancing by one.
+template <typename T, int KIND, int OV, bool MONO>
+__device__ __forceinline__ void red_cols(const RedParams& p, const T* __restrict__ in, int64_t base,
+                                         typename RedLocal<T, KIND>::Local (&acc)[OV]) {
+    using R = RedLocal<T, KIND>;
+    const int64_t rb = (int64_t)blockIdx.y * p.chunk;
+    const int64_t re = min(p.nred, rb + p.chunk);
+    if (rb >= re) return;
+    const uint32_t n0 = p.r.shape[0];
+    const int64_t s0 = p.r.stride[0];
+    const uint32_t l0 = (uint32_t)p.r.lstride[0];
+    uint32_t row = p.r.div[0].div((uint32_t)rb);
+    uint32_t c = (uint32_t)rb - row * n0;
+    uint32_t lrow;
+    int64_t roff = red_row_offset(p.r, row, &lrow);
+    for (int64_t r = rb; r < re; r += kRedUnrollCol) {
+        RVec<T, OV> v[kRedUnrollCol];
+        uint32_t li[kRedUnrollCol];
+#pragma unroll
+        for (int u = 0; u < kRedUnrollCol; ++u) {
+            if (r + u < re) {
+                li[u] = MONO ? (uint32_t)(r + u) : lrow + c * l0;
+                v[u] = *reinterpret_cast<const RVec<T, OV>*>(in + base + roff + (int64_t)c * s0);
+                if (++c == n0) {
+                    c = 0;
+                    ++row;
+                    if (r + u + 1 < re) roff = red_row_offset(p.r, row, &lrow);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kRedUnrollCol; ++u)
+            if (r + u < re) {
+#pragma unroll
+                for (int j = 0; j < OV; ++j) {
+                    if constexpr (R::kArg && MONO) {
+                        // logical indices increase along the walk: a later
+                        // equal key never wins
+                        const typename R::Key k = R::key(v[u].v[j]);
+                        const bool take = R::kwins(k, acc[j].v);
+                        acc[j].v = take ? k : acc[j].v;
+                        acc[j].idx = take ? li[u] : acc[j].idx;
+                    } else {
+                        R::lfold(acc[j], v[u].v[j], li[u]);
+                    }
+                }
+            }
+    }
+}
+
+// Arg reductions: a NaN at logical index 0 (flattened reduced index 0, the
+// element at the output's base offset) makes the answer 0; tested once per
+// output by the thread that owns reduced index 0.
 template <typename T, int KIND>
-__global__ void __launch_bounds__(kRedThreads) reduce_kernel(const RedParams p) {
-    if (p.ocol > 1) {
-        if constexpr (red_col_vec<T>() > 1) reduce_colvec<T, KIND>(p);
+__device__ __forceinline__ void red_nan0(typename RedLocal<T, KIND>::Acc& acc, const T* __restrict__ in,
+                                         int64_t base) {
+    if constexpr (RedLocal<T, KIND>::kArg) {
+        if (blockIdx.y == 0) {
+            const T x = in[base];
+            if (is_nan_v(x)) acc.nan0 = 1;
+        }
+    }
+}
+
+template <typename T, int KIND>
+__device__ __forceinline__ void red_store(const RedParams& p, int64_t o, const typename Red<T, KIND>::Acc& acc) {
+    using R = Red<T, KIND>;
+    if (p.partial) {
+        reinterpret_cast<typename R::Acc*>(p.partial)[(int64_t)blockIdx.y * p.nout + o] = acc;
         return;
     }
-    using R = Red<T, KIND>;
+    reinterpret_cast<typename R::Out*>(p.out)[p.out_off + kept_offset(p.k, (uint32_t)o, true)] =
+        R::fin(acc, p.op, p.nred);
+}
+
+// Column regime: one thread per output, or per OV neighbouring outputs.
+template <typename T, int KIND, int OV, bool MONO>
+__global__ void __launch_bounds__(kRedThreads) reduce_col_kernel(const RedParams p) {
+    using R = RedLocal<T, KIND>;
     using Acc = typename R::Acc;
-    constexpr int VEC = 16 / sizeof(T) > 0 ? 16 / sizeof(T) : 1;
+    const T* __restrict__ in = reinterpret_cast<const T*>(p.in);
+    const int64_t o0 = ((int64_t)blockIdx.x * kRedThreads + threadIdx.x) * OV;
+    if (o0 >= p.nout) return;  // with OV > 1, nout is a multiple of OV
+    const int64_t base = p.in_off + kept_offset(p.k, (uint32_t)o0, false);
+    typename R::Local acc[OV];
+#pragma unroll
+    for (int j = 0; j < OV; ++j) acc[j] = R::linit();
+    red_cols<T, KIND, OV, MONO>(p, in, base, acc);
+#pragma unroll
+    for (int j = 0; j < OV; ++j) {
+        Acc a = R::to_acc(acc[j]);
+        red_nan0<T, KIND>(a, in, base + (int64_t)j);  // kept dim 0 is contiguous when OV > 1
+        red_store<T, KIND>(p, o0 + j, a);
+    }
+}
+
+// Row regime: a group of G = 2^glog threads per output (G may be 1).
+template <typename T, int KIND, int W, bool MONO>
+__global__ void __launch_bounds__(kRedThreads) reduce_row_kernel(const RedParams p) {
+    using R = RedLocal<T, KIND>;
+    using Acc = typename R::Acc;
+    const T* __restrict__ in = reinterpret_cast<const T*>(p.in);
     const int G = 1 << p.glog;
     const int tid = threadIdx.x;
     const int lane = tid & (G - 1);
     const int64_t o = (int64_t)blockIdx.x * (kRedThreads >> p.glog) + (tid >> p.glog);
     const bool active = o < p.nout;
-    const T* __restrict__ in = reinterpret_cast<const T*>(p.in);
-
+    int64_t base = 0;
     Acc acc = R::init();
     if (active) {
-        // input base of this output element
-        int64_t base = p.in_off;
-        {
-            uint32_t e = (uint32_t)o;
-            for (int i = 0; i < p.k.nd - 1; ++i) {
-                uint32_t q = p.k.div[i].div(e);
-                base += (int64_t)(e - q * p.k.shape[i]) * p.k.in_stride[i];
-                e = q;
-            }
-            if (p.k.nd > 0) base += (int64_t)e * p.k.in_stride[p.k.nd - 1];
-        }
-        const int64_t rb = (int64_t)blockIdx.y * p.chunk;
-        const int64_t re = min(p.nred, rb + p.chunk);
-        // kRedUnroll independent loads are issued before they are folded, so
-        // each thread keeps several requests in flight
-        if (VEC > 1 && p.vec) {
-            const int64_t step = (int64_t)G * VEC;
-            for (int64_t r0 = rb + (int64_t)lane * VEC; r0 < re; r0 += step * kRedUnroll) {
-                RVec<T, VEC> v[kRedUnroll];
-                int64_t li[kRedUnroll];
-#pragma unroll
-                for (int u = 0; u < kRedUnroll; ++u) {
-                    const int64_t r = r0 + u * step;
-                    if (r < re) {
-                        const int64_t off = red_offset(p.r, (uint32_t)r, &li[u]);
-                        v[u] = *reinterpret_cast<const RVec<T, VEC>*>(in + base + off);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < kRedUnroll; ++u) {
-                    if (r0 + u * step < re) {
-#pragma unroll
-                        for (int j = 0; j < VEC; ++j) R::fold(acc, v[u].v[j], li[u] + j * p.r.lstride[0]);
-                    }
-                }
-            }
-        } else {
-            for (int64_t r0 = rb + lane; r0 < re; r0 += (int64_t)G * kRedUnroll) {
-                T x[kRedUnroll];
-                int64_t li[kRedUnroll];
-#pragma unroll
-                for (int u = 0; u < kRedUnroll; ++u) {
-                    const int64_t r = r0 + (int64_t)u * G;
-                    if (r < re) x[u] = in[base + red_offset(p.r, (uint32_t)r, &li[u])];
-                }
-#pragma unroll
-                for (int u = 0; u < kRedUnroll; ++u)
-                    if (r0 + (int64_t)u * G < re) R::fold(acc, x[u], li[u]);
-            }
-        }
+        base = p.in_off + kept_offset(p.k, (uint32_t)o, false);
+        acc = R::to_acc(red_rows<T, KIND, W, MONO>(p, in, base, lane, G));
     }
     // combine the group (fixed tree: deterministic)
-    if (G > 1) {
-        const int width = G < 32 ? G : 32;
-        for (int d = width >> 1; d > 0; d >>= 1) {
-            Acc other = shfl_down_acc(acc, d, width);
-            R::merge(acc, other);
-        }
-        if (G > 32) {
-            __shared__ Acc warp_acc[kRedThreads / 32];
-            const int w = tid >> 5;
-            if ((tid & 31) == 0) warp_acc[w] = acc;
-            __syncthreads();
-            if (tid == 0) {
-                acc = warp_acc[0];
-                for (int i = 1; i < kRedThreads / 32; ++i) R::merge(acc, warp_acc[i]);
-            }
+    const int width = G < 32 ? G : 32;
+    for (int d = width >> 1; d > 0; d >>= 1) {
+        Acc other = shfl_down_acc(acc, d, width);
+        R::merge(acc, other);
+    }
+    if (G > 32) {
+        // a group spans G / 32 warps: its lane 0 folds those warps' partials
+        __shared__ Acc warp_acc[kRedThreads / 32];
+        const int w = tid >> 5;
+        if ((tid & 31) == 0) warp_acc[w] = acc;
+        __syncthreads();
+        if (lane == 0) {
+            const int nw = G >> 5;
+            for (int i = 1; i < nw; ++i) R::merge(acc, warp_acc[w + i]);
         }
     }
     if (!active || lane != 0) return;
-    if (p.partial) {
-        reinterpret_cast<Acc*>(p.partial)[(int64_t)blockIdx.y * p.nout + o] = acc;
-        return;
-    }
-    int64_t oo = p.out_off;
-    {
-        uint32_t e = (uint32_t)o;
-        for (int i = 0; i < p.k.nd - 1; ++i) {
-            uint32_t q = p.k.div[i].div(e);
-            oo += (int64_t)(e - q * p.k.shape[i]) * p.k.out_stride[i];
-            e = q;
+    red_nan0<T, KIND>(acc, in, base);
+    red_store<T, KIND>(p, o, acc);
+}
+
+// Launch the main pass of a planned reduction (partials already assigned):
+// the regime's kernel, with vector loads and the ordered fold where the plan
+// allows them (the ordered fold matters only to the arg reductions).
+template <typename T, int KIND>
+cudaError_t launch_reduce_pass(const RedParams& p, dim3 grid, cudaStream_t stream) {
+    constexpr int VEC = 16 / sizeof(T) > 0 ? 16 / sizeof(T) : 1;
+    constexpr int OV = red_col_vec<T>();
+    constexpr bool kArg = RedLocal<T, KIND>::kArg;
+    const bool mono = kArg && p.mono;
+    if (p.row) {
+        if (VEC > 1 && p.vec) {
+            if (mono)
+                reduce_row_kernel<T, KIND, VEC, kArg><<<grid, kRedThreads, 0, stream>>>(p);
+            else
+                reduce_row_kernel<T, KIND, VEC, false><<<grid, kRedThreads, 0, stream>>>(p);
+        } else {
+            if (mono)
+                reduce_row_kernel<T, KIND, 1, kArg><<<grid, kRedThreads, 0, stream>>>(p);
+            else
+                reduce_row_kernel<T, KIND, 1, false><<<grid, kRedThreads, 0, stream>>>(p);
         }
-        if (p.k.nd > 0) oo += (int64_t)e * p.k.out_stride[p.k.nd - 1];
+    } else if (OV > 1 && p.ocol > 1) {
+        if (mono)
+            reduce_col_kernel<T, KIND, OV, kArg><<<grid, kRedThreads, 0, stream>>>(p);
+        else
+            reduce_col_kernel<T, KIND, OV, false><<<grid, kRedThreads, 0, stream>>>(p);
+    } else {
+        if (mono)
+            reduce_col_kernel<T, KIND, 1, kArg><<<grid, kRedThreads, 0, stream>>>(p);
+        else
+            reduce_col_kernel<T, KIND, 1, false><<<grid, kRedThreads, 0, stream>>>(p);
     }
-    reinterpret_cast<typename R::Out*>(p.out)[oo] = R::fin(acc, p.op, p.nred);
+    return cudaGetLastError();
 }
 
 // Fold the per-chunk accumulators of every output in chunk order.
@@ -619,8 +797,8 @@ int launch_reduce(rstsr_ctx* ctx, RedParams p) {
     } else {
         p.partial = nullptr;
     }
-    reduce_kernel<T, KIND><<<dim3((unsigned)gx, (unsigned)p.nsplit), kRedThreads, 0, ctx->stream>>>(p);
-    int s = after_launch(ctx, "reduce_kernel");
+    cudaError_t e = launch_reduce_pass<T, KIND>(p, dim3((unsigned)gx, (unsigned)p.nsplit), ctx->stream);
+    int s = e == cudaSuccess ? after_launch(ctx, "reduce pass") : cuda_fail(e, "reduce pass");
     if (s == RSTSR_OK && p.nsplit > 1) {
         const int64_t gc = (p.nout + kRedThreads - 1) / kRedThreads;
         reduce_combine_kernel<T, KIND><<<(unsigned)gc, kRedThreads, 0, ctx->stream>>>(p);

@@ -194,3 +194,28 @@ def test_kat_reductions(dev, kats):
             got = getattr(t, op)(case["axes"]).to_numpy()
             np.testing.assert_allclose(got.astype(np.float64), np.array(case["expect"], dtype=np.float64), rtol=1e-13,
                                        err_msg=case["src"])
+
+
+# reduced lengths that select every group size of the row regime (one thread
+# per output up to 256 threads per output, several outputs per CTA) and the
+# column regime, with a few outputs each, against the oracle
+@pytest.mark.parametrize("nred", [7, 100, 1000, 2500, 5000, 8192, 20000, 70001])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32, np.int64])
+@pytest.mark.parametrize("order", ["C", "F"])
+def test_group_sizes_match_oracle(dev, nred, dtype, order):
+    shape = (5, nred)
+    stride = OL.c_stride(shape) if order == "C" else OL.f_stride(shape)
+    buf = rand(shape, dtype, seed=nred).ravel()
+    if np.dtype(dtype).kind == "i":
+        buf[:] = buf % 17  # ties for the arg reductions
+    case = (buf, shape, stride, 0)
+    t = up(dev, *case)
+    for op in ("sum", "max"):
+        want, lo = oracle_reduce(op, case, [1], dtype)
+        got = rt.reduce_axes(op, t, [1])
+        assert (got.shape, got.stride) == lo
+        check_close(got.to_numpy(), want, dtype, op)
+    for is_max in (True, False):
+        out = O.empty_strided((5,), (1,), np.uint64)
+        O.argreduce_axes(is_max, O.Strided(*case), [1], out, nthreads=4)
+        np.testing.assert_array_equal(rt.argreduce_axes(is_max, t, [1]).to_numpy(), out.values())
