@@ -46,6 +46,8 @@ N = int(np.prod(SHAPE))
 DTYPES = [("f64", np.float64), ("f32", np.float32), ("i32", np.int32)]
 LAYOUTS = ["c", "f", "perm", "slice"]
 METRIC = "f64 GEMM TFLOP/s Ozaki-split vs native FP64 at ≤1e-12 rel err; elementwise HBM GB/s"
+WORKLOAD = ("strided ops [32,64,128,128] x {f64,f32,i32} x {C,F,permuted,step-2 slice}: "
+            "permute(0,2,1,3)+to_contig, a*b+c (c [1,64,1,128]), sum(1,3), argmax(-1)")
 
 
 def c_stride(shape):
@@ -355,6 +357,7 @@ def run_gpu(args):
                 traffic = json.loads(tpath.read_text()).get("fma_f64_c")
             except Exception:
                 traffic = None
+        details = {"per_op": per_op, "per_case": per_case}
         result = {
             "metric": METRIC,
             "value": round(value, 1),
@@ -368,9 +371,9 @@ def run_gpu(args):
             "vs_baseline": None,
             "dtype": "f64,f32,i32",
             "data": "synthetic (seeded uniform; i32 uniform in [-1000,1000])",
+            "gpu_launches": int(launches),
             "config": {
-                "workload": "strided ops [32,64,128,128] x {f64,f32,i32} x {C,F,permuted,step-2 slice}: "
-                            "permute(0,2,1,3)+to_contig, a*b+c (c [1,64,1,128]), sum(1,3), argmax(-1)",
+                "workload": WORKLOAD,
                 "l2": "inputs larger than L2 (>=128 MiB per tensor), no flush",
                 "parallelism": f"replicas x{world}",
                 "step_bytes": step_bytes,
@@ -387,25 +390,54 @@ def run_gpu(args):
                 "algorithmic_bytes_per_launch": fma_bytes,
                 "avg_launch_ms": round(fma_ms, 4),
             },
-            "per_op": per_op,
-            "per_case": per_case,
-            "gpu_launches": int(launches),
             "e2e": e2e,
             "clocks": clocks.summary() if clocks else None,
+            # fraction of the measured HBM bandwidth per operation over all cases
+            "per_op_frac_hbm": {op: round(v["gbs"] / peak, 3) for op, v in per_op.items()},
         }
-        if not args.no_gemm:
-            result["gemm"] = run_gemm_section(dev, stream)
-            result["gemm"].update(run_batched_section(dev, stream))
-            result["small_f64"] = run_small_section(dev, stream)
-            result["tri_index"] = run_tri_index_section(dev, stream)
-            result["contraction"] = run_contraction_section(dev, stream)
-            result["contraction"].update(run_blas3_section(dev, stream))
         if not args.no_cpu:
-            result["cpu_baseline"] = cpu_baseline(args)
+            result["cpu_baseline"], result["parity"] = cpu_baseline(args, wl)
+        if not args.no_gemm:
+            gemm = run_gemm_section(dev, stream)
+            gemm.update(run_batched_section(dev, stream))
+            details["gemm"] = gemm
+            details["small_f64"] = run_small_section(dev, stream)
+            details["tri_index"] = run_tri_index_section(dev, stream)
+            details["contraction"] = run_contraction_section(dev, stream)
+            details["contraction"].update(run_blas3_section(dev, stream))
+            result["details_file"] = "bench_details.json (RSTSR_BENCH_OUT, else the temp directory)"
+            # the GEMM half of the metric, compact and last on the line
+            result["gemm"] = gemm_summary(gemm, details["small_f64"])
+        (out_dir / "bench_details.json").write_text(json.dumps(details, indent=1))
     if world > 1:
         torch.distributed.barrier()
         torch.distributed.destroy_process_group()
     return result
+
+
+def gemm_summary(g, small):
+    """The headline GEMM numbers (full entries in the details file)."""
+    c3 = g["c3_ozaki_f64"]
+    out = {}
+    for name in ("c4_split_f32_8192", "c4_split_f32_tall"):
+        e = g[name]
+        out[name] = {"tflops": e["tflops"], "rel_err": float(f"{e['rel_err_vs_fp64']:.3g}"),
+                     "sgemm_tflops": e["cublas_sgemm_tflops"],
+                     "bf16x9_tflops": e.get("cublas_emulated_bf16x9", {}).get("tflops")}
+    gr, bc, ch = g["c5_grouped_f64_512"], g["c5_broadcast_batch_f64"], g["c5_graph_chain_f64"]
+    out["c5"] = {"grouped_tflops": gr["tflops"], "grouped_err": float(f"{gr['rel_err_frobenius']:.3g}"),
+                 "grouped_launches": gr["launches_per_call"], "tuned": gr.get("tuned", False),
+                 "bcast_tflops": bc["tflops"], "bcast_err": float(f"{bc['rel_err_frobenius']:.3g}"),
+                 "graph_us": ch["graph_us_per_iter"], "eager_us": ch["eager_us_per_iter"]}
+    out["c1_small_f64"] = {"exact_add": small["add_bit_exact"], "exact_argmax": small["argmax_exact"],
+                           "matmul_err": float(f"{small['matmul_rel_err']:.3g}")}
+    out["c3_ozaki_f64"] = {
+        "tflops": c3["tflops"], "ms": c3["ms"], "slices": c3["slices"],
+        "rel_err": float(f"{c3['rel_err_frobenius']:.3g}"),
+        "dgemm_tflops": c3["native_fp64_cublas_tflops"], "dsyrk_tflops": c3.get("native_dsyrk_tflops"),
+        "speedup_vs_dgemm": c3["speedup_vs_native_fp64"], "speedup_vs_dsyrk": c3.get("speedup_vs_native_dsyrk"),
+        "tensor_frac": c3["roofline"]["frac"]}
+    return out
 
 
 def _time_events(stream, fn, reps):
@@ -431,15 +463,7 @@ class _CublasEmulated:
     F64_FIXEDPOINT, F32_BF16X9 = 79, 78
 
     def __init__(self, stream):
-        lib = None
-        for name in ("libcublas.so.13", "/usr/local/cuda/lib64/libcublas.so.13"):
-            try:
-                lib = C.CDLL(name)
-                break
-            except OSError:
-                continue
-        if lib is None:
-            raise RuntimeError("libcublas.so.13 not found")
+        lib = _cublas_lib()
         self.lib = lib
         self.h = C.c_void_p()
         if lib.cublasCreate_v2(C.byref(self.h)) != 0:
@@ -462,6 +486,49 @@ class _CublasEmulated:
 
     def close(self):
         self.lib.cublasDestroy_v2(self.h)
+
+
+def _cublas_lib():
+    for name in ("libcublas.so.13", "/usr/local/cuda/lib64/libcublas.so.13"):
+        try:
+            return C.CDLL(name)
+        except OSError:
+            continue
+    raise RuntimeError("libcublas.so.13 not found")
+
+
+def _cublas_dsyrk(stream, x, n, k, ref):
+    """cuBLAS DSYRK (native FP64) of C = X X^T, X the column-major [n, k] view
+    of the row-major [k, n] tensor `x`, lower triangle; returns (seconds,
+    relative Frobenius error of that triangle against `ref`)."""
+    import torch
+
+    lib = _cublas_lib()
+    h = C.c_void_p()
+    if lib.cublasCreate_v2(C.byref(h)) != 0:
+        raise RuntimeError("cublasCreate failed")
+    try:
+        lib.cublasSetStream_v2(h, C.c_void_p(stream.cuda_stream))
+        lib.cublasDsyrk_v2.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_int]
+        c = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        one, zero = C.c_double(1.0), C.c_double(0.0)
+
+        def run():
+            st = lib.cublasDsyrk_v2(h, 0, 0, n, k, C.byref(one), C.c_void_p(x.data_ptr()), n, C.byref(zero),
+                                    C.c_void_p(c.data_ptr()), n)
+            if st != 0:
+                raise RuntimeError(f"cublasDsyrk returned {st}")
+
+        sec = _time_events(stream, run, 1)
+        # the column-major lower triangle is the upper triangle of the row-major view
+        tri = torch.triu(c)
+        rtri = torch.triu(ref)
+        err = (torch.linalg.norm(tri - rtri) / torch.linalg.norm(rtri)).item()
+        del c, tri, rtri
+        return sec, err
+    finally:
+        lib.cublasDestroy_v2(h)
 
 
 def run_gemm_section(dev, stream):
@@ -511,6 +578,16 @@ def run_gemm_section(dev, stream):
                      "unit": "TFLOP/s", "frac": round(bf16_flops / sec / 1e12 / peak, 3),
                      "peak_source": peak_src, "work": "bf16 slice products of the computed tiles"},
     }
+    # native comparator on the reference's own path (SYRK: only one triangle
+    # is computed, as the reference's B^T B does): cuBLAS DSYRK, C = X X^T with
+    # X the column-major [15000, 1000] view of Bm, lower triangle
+    try:
+        sec_syrk, err_syrk = _cublas_dsyrk(stream, tb, Q, P, ref)
+        out["c3_ozaki_f64"].update({
+            "native_dsyrk_tflops": round(flops / sec_syrk / 1e12, 3), "native_dsyrk_ms": round(sec_syrk * 1e3, 2),
+            "native_dsyrk_rel_err_triangle": err_syrk, "speedup_vs_native_dsyrk": round(sec_syrk / sec, 1)})
+    except Exception as exc:
+        out["c3_ozaki_f64"]["native_dsyrk"] = {"unavailable": str(exc)[:200]}
     # comparator: cuBLAS's own fixed-point FP64 emulation, C = X X^T with X the
     # column-major [15000, 1000] view of Bm
     try:
@@ -580,6 +657,51 @@ def run_gemm_section(dev, stream):
     return out
 
 
+def run_rates(args):
+    """Dense tensor-core rates that decide the slice type of the split GEMMs
+    on this GPU: INT8 (torch._int_mm, int32 accumulation), BF16 and FP16
+    (torch.matmul, fp32 accumulation) and native FP64 (torch.matmul, cuBLAS
+    DGEMM), all n^3 with n = --rate-n, CUDA events, best of the timed calls."""
+    import torch
+
+    n = args.rate_n
+    stream = torch.cuda.current_stream()
+    res = {"n": n}
+    g = torch.Generator(device="cuda").manual_seed(0)
+
+    def best(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t.append(e0.elapsed_time(e1) * 1e-3)
+        return min(t)
+
+    a8 = torch.randint(-128, 128, (n, n), dtype=torch.int8, device="cuda", generator=g)
+    b8 = torch.randint(-128, 128, (n, n), dtype=torch.int8, device="cuda", generator=g)
+    try:
+        res["int8_tops"] = round(2.0 * n ** 3 / best(lambda: torch._int_mm(a8, b8), 10) / 1e12, 1)
+    except Exception as exc:
+        res["int8_tops"] = f"unavailable: {str(exc)[:120]}"
+    del a8, b8
+    for name, dt in (("bf16_tflops", torch.bfloat16), ("fp16_tflops", torch.float16)):
+        x = torch.rand((n, n), dtype=dt, device="cuda", generator=g)
+        y = torch.rand((n, n), dtype=dt, device="cuda", generator=g)
+        res[name] = round(2.0 * n ** 3 / best(lambda: x @ y, 10) / 1e12, 1)
+        del x, y
+    x = torch.rand((n, n), dtype=torch.float64, device="cuda", generator=g)
+    y = torch.rand((n, n), dtype=torch.float64, device="cuda", generator=g)
+    res["fp64_tflops"] = round(2.0 * n ** 3 / best(lambda: x @ y, 2) / 1e12, 3)
+    res["torch"] = torch.__version__
+    res["gpu"] = torch.cuda.get_device_name(0)
+    return {"section": "tensor_rates", "results": res}
+
+
 def run_c3_only(args):
     """Only the Ozaki contraction C = Bm^T Bm with Bm [1000, cols] (cols =
     15000 is the full workload; smaller for profiling), timed over --steps
@@ -637,6 +759,13 @@ def run_batched_section(dev, stream):
         flops += 2.0 * m * n * k
     arr = (GemmProblem * len(probs))(*probs)
     run = lambda: call("rstsr_cuda_gemm_grouped", dev.ctx, 0, arr, len(probs), None)
+    run()
+    torch.cuda.synchronize()
+    # tile configuration from the project's autotuner, for the shape class of
+    # the call (its largest m, n, k) at the slice count the call chose
+    sl = int(rt.lib().rstsr_cuda_last_ozaki_slices())
+    mx = [int(v) for v in dims.max(axis=0)]
+    tuned = rt.autotune_gemm(dev, np.float64, mx[0], mx[1], mx[2], slices=sl)
     l0 = dev.launch_count()
     run()
     torch.cuda.synchronize()
@@ -649,7 +778,8 @@ def run_batched_section(dev, stream):
         den += float(np.sum(r * r))
     out["c5_grouped_f64_512"] = {"tflops": round(flops / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
                                  "sum_2mnk": flops, "rel_err_frobenius": (num / den) ** 0.5,
-                                 "launches_per_call": int(launches)}
+                                 "launches_per_call": int(launches), "slices": sl, "tuned": True,
+                                 "tuned_config": {"shape_class": mx, "k_tile": tuned & 0xFF, "group": tuned >> 8}}
     del keep, probs, arr
     # (ii) broadcast batch
     a = rng.uniform(-1, 1, (64, 1, 256, 256))
@@ -657,6 +787,10 @@ def run_batched_section(dev, stream):
     ta, tb = rt.asarray(a, dev), rt.asarray(b, dev)
     tc = rt.empty((64, 32, 256, 256), np.float64, dev)
     run = lambda: rt.matmul_into(tc, ta, tb)
+    run()
+    torch.cuda.synchronize()
+    sl = int(rt.lib().rstsr_cuda_last_ozaki_slices())
+    tuned = rt.autotune_gemm(dev, np.float64, 256, 256, 256, slices=sl)
     l0 = dev.launch_count()
     run()
     torch.cuda.synchronize()
@@ -670,7 +804,8 @@ def run_batched_section(dev, stream):
     out["c5_broadcast_batch_f64"] = {
         "shape": "[64,1,256,256] % [1,32,256,256]", "tflops": round(flops / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
         "rel_err_frobenius": (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item(),
-        "native_fp64_cublas_tflops": round(flops / sec_ref / 1e12, 3), "launches_per_call": int(launches)}
+        "native_fp64_cublas_tflops": round(flops / sec_ref / 1e12, 3), "launches_per_call": int(launches),
+        "slices": sl, "tuned": True, "tuned_config": {"k_tile": tuned & 0xFF, "group": tuned >> 8}}
     del ta, tb, tc, ga, gb, ref, got
     torch.cuda.empty_cache()
     # (iii) graph-captured chain
@@ -966,43 +1101,53 @@ def run_tri_index_only(args):
 
 
 def run_e2e(wl, dev, stream, args, world):
-    """Same step with host buffers: every input copied in (pinned host memory)
-    and every result copied out inside the timed region, through the C ABI."""
+    """Same step with host buffers, through the C ABI's host-transfer entry
+    points: every input copied in (rstsr_cuda_memcpy_h2d_async) and every
+    result copied out (rstsr_cuda_memcpy_d2h_async) inside the timed region,
+    which ends when the last result is on the host. Two host-memory kinds:
+    page-locked buffers (one stream-ordered copy each; copies in, compute and
+    copies out of successive cases overlap on three streams) and pageable
+    numpy buffers, what a Rust Vec<T> is (chunked staging through the
+    context's page-locked ring; the host waits for each result)."""
     import torch
 
     lib = wl.lib
-    pinned = []
-    for c in wl.cases:
-        ha = torch.from_numpy(c["ha"]).pin_memory()
-        hb = torch.from_numpy(c["hb"]).pin_memory()
-        hc = torch.from_numpy(np.ascontiguousarray(c["hc"])).pin_memory()
-        outs = dict(
-            perm=torch.empty(c["out_perm"].size * c["esize"], dtype=torch.uint8).pin_memory(),
-            d=torch.empty(wl_bytes(c["d"]), dtype=torch.uint8).pin_memory(),
-            s=torch.empty(wl_bytes(c["sum_out"]), dtype=torch.uint8).pin_memory(),
-            g=torch.empty(wl_bytes(c["arg_out"]), dtype=torch.uint8).pin_memory(),
-        )
-        pinned.append((ha, hb, hc, outs))
+    n = len(wl.cases)
 
-    # three streams: inputs in, compute, results out; case i+1 uploads while
-    # case i computes and earlier results download (the C2C link is full duplex).
-    # The context's stream is switched per phase (rstsr_cuda_ctx_set_stream);
-    # events order the phases of one case.
+    def outs_of(c, alloc):
+        return {k: alloc(b) for k, b in (("perm", c["out_perm"].size * c["esize"]), ("d", wl_bytes(c["d"])),
+                                         ("s", wl_bytes(c["sum_out"])), ("g", wl_bytes(c["arg_out"])))}
+
+    pinned, pageable = [], []
+    for c in wl.cases:
+        pin = lambda b: torch.empty(b, dtype=torch.uint8).pin_memory()
+        pinned.append(([torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in (c["ha"], c["hb"], c["hc"])],
+                       outs_of(c, pin)))
+        pageable.append(([np.ascontiguousarray(x) for x in (c["ha"], c["hb"], c["hc"])],
+                         outs_of(c, lambda b: np.empty(b, dtype=np.uint8))))
+
+    def addr(x):
+        return x.data_ptr() if isinstance(x, torch.Tensor) else x.ctypes.data
+
+    def nbytes(x):
+        return x.numel() * x.element_size() if isinstance(x, torch.Tensor) else x.nbytes
+
+    # three streams: inputs in, compute, results out; the context's stream is
+    # switched per phase (rstsr_cuda_ctx_set_stream), events order the phases
     s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
     s_comp = stream
-    n = len(wl.cases)
     ev_in = [torch.cuda.Event() for _ in range(n)]
     ev_comp = [torch.cuda.Event() for _ in range(n)]
 
-    def step():
+    def step(bufs):
         h2d = d2h = 0
-        for i, (c, (ha, hb, hc, outs)) in enumerate(zip(wl.cases, pinned)):
+        for i, (c, (ins, outs)) in enumerate(zip(wl.cases, bufs)):
             dev.set_stream(s_in.cuda_stream)
-            for host, t in ((ha, c["a"]), (hb, c["b"]), (hc, c["c"])):
-                nb = host.numel() * host.element_size()
-                rc = lib.rstsr_cuda_memcpy_h2d(dev.ctx, C.c_void_p(t.ptr), C.c_void_p(host.data_ptr()), C.c_size_t(nb))
-                assert rc == 0
-                h2d += nb
+            for host, t in zip(ins, (c["a"], c["b"], c["c"])):
+                rc = lib.rstsr_cuda_memcpy_h2d_async(dev.ctx, C.c_void_p(t.ptr), C.c_void_p(addr(host)),
+                                                     C.c_size_t(nbytes(host)))
+                assert rc == 0, lib.rstsr_cuda_last_error().decode()
+                h2d += nbytes(host)
             ev_in[i].record(s_in)
             s_comp.wait_event(ev_in[i])
             dev.set_stream(s_comp.cuda_stream)
@@ -1015,26 +1160,31 @@ def run_e2e(wl, dev, stream, args, world):
                            ("g", c["arg_out"])):
                 if t is None:
                     continue
-                nb = outs[key].numel()
-                # asynchronous device->host copy (pinned destination)
-                rc = lib.rstsr_cuda_memcpy_d2d(dev.ctx, C.c_void_p(outs[key].data_ptr()), C.c_void_p(t.ptr),
-                                               C.c_size_t(nb))
-                assert rc == 0
-                d2h += nb
+                rc = lib.rstsr_cuda_memcpy_d2h_async(dev.ctx, C.c_void_p(addr(outs[key])), C.c_void_p(t.ptr),
+                                                     C.c_size_t(nbytes(outs[key])))
+                assert rc == 0, lib.rstsr_cuda_last_error().decode()
+                d2h += nbytes(outs[key])
         dev.set_stream(s_comp.cuda_stream)
         return h2d, d2h
 
-    for _ in range(max(1, args.warmup // 2)):
-        step()
-        torch.cuda.synchronize()
-    steps = max(1, min(args.steps, 3))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        h2d, d2h = step()
-        torch.cuda.synchronize()  # a step ends when its last result is on the host
-    rate, t = replicas.whole_job_rate(wl.total_bytes(), (time.perf_counter() - t0) / steps, "cuda")
-    return {"value": round(rate / 1e9, 1), "unit": "GB/s",
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 3)}
+    steps = max(10, min(args.steps, 20))
+    res = {}
+    for name, bufs in (("pinned", pinned), ("pageable", pageable)):
+        for _ in range(max(1, args.warmup // 2)):
+            step(bufs)
+            torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            h2d, d2h = step(bufs)
+            torch.cuda.synchronize()  # a step ends when its last result is on the host
+        rate, t = replicas.whole_job_rate(wl.total_bytes(), (time.perf_counter() - t0) / steps, "cuda")
+        res[name] = {"value": round(rate / 1e9, 1), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
+                     "d2h_bytes_per_step": int(d2h), "ms_per_step": round(t * 1e3, 3), "steps": steps}
+    dev.set_stream(stream.cuda_stream)
+    out = dict(res["pinned"])
+    out["host_memory"] = "page-locked (pinned); wall clock over the timed steps"
+    out["pageable"] = {k: res["pageable"][k] for k in ("value", "ms_per_step")}
+    return out
 
 
 def wl_bytes(t):
@@ -1050,46 +1200,71 @@ def wl_bytes(t):
 # ------------------------------------------------------------ CPU legs
 
 
-def cpu_sample_step(batch, nthreads, seed=0, reps=1):
-    """One bounded sample of the step on the CPU oracle (OpenMP restatement of
-    the reference's rayon kernels): the first `batch` of the 32 leading
-    indices, all dtypes and layouts, each case's operations timed `reps`
-    times. Returns (seconds, algorithmic bytes)."""
+def host_cases(seed=0, src=None, batch=32):
+    """Host inputs of every (dtype, layout) case of the step, restricted to
+    the leading `batch` of the 32 indices of axis 0 (a view with the full
+    tensor's strides). `src` is the GPU workload, whose own host buffers are
+    then used; otherwise the buffers are generated with the workload's seeds."""
+    shape = (batch,) + SHAPE[1:]
+    out = []
+    for di, (dname, dt) in enumerate(DTYPES):
+        for li, kind in enumerate(LAYOUTS):
+            if src is not None:
+                c = next((x for x in src.cases if x["dname"] == dname and x["kind"] == kind), None)
+                if c is None:
+                    continue
+                ha, hb, hc = c["ha"], c["hb"], c["hc"]
+            else:
+                blen, _, _ = layout_of(kind, SHAPE)
+                ha = host_data(dt, blen, seed + 10 * di + li)
+                hb = host_data(dt, blen, seed + 1000 + 10 * di + li)
+                hc = host_data(dt, int(np.prod(CSHAPE)), seed + 100 + di)
+            _, stride, off = layout_of(kind, SHAPE)
+            out.append(dict(dname=dname, kind=kind, dt=dt, esize=np.dtype(dt).itemsize, shape=shape, stride=stride,
+                            off=off, ha=ha, hb=hb, hc=hc))
+    return out
+
+
+def cpu_step(cases, nthreads, reps=1, keep=False):
+    """The step's operations on the CPU oracle (OpenMP restatement of the
+    reference's rayon kernels) over `cases`, each case's operations timed
+    `reps` times. The reference's two passes for a*b+c: tmp = a*b in the
+    binary-op layout, then tmp += c. Returns (seconds, algorithmic bytes,
+    outputs of the last repetition per case if `keep`)."""
+    from oracle import layout as OL
     from oracle import oracle as O
 
-    shape = (batch,) + SHAPE[1:]
-    n = int(np.prod(shape))
-    tot_t, tot_b = 0.0, 0
-    for di, (dname, dt) in enumerate(DTYPES):
-        esize = np.dtype(dt).itemsize
-        cbuf = host_data(dt, int(np.prod(CSHAPE)), seed + 100 + di)
-        for li, kind in enumerate(LAYOUTS):
-            blen, stride, off = layout_of(kind, shape)
-            a = O.Strided(host_data(dt, blen, seed + 10 * di + li), shape, stride, off)
-            b = O.Strided(host_data(dt, blen, seed + 1000 + 10 * di + li), shape, stride, off)
-            cst = O.Strided(cbuf, shape, (0, CSHAPE[3], 0, 1), 0)
-            pshape, pstride = permuted_view(shape, stride)
-            for _ in range(reps):
-                t0 = time.perf_counter()
-                if kind != "perm":
-                    dst = O.empty_strided(pshape, c_stride(pshape), dt)
-                    O.assign_arbitrary(dst, O.Strided(a.buf, pshape, pstride, off), 0, nthreads)
-                # the reference's two passes: tmp = a*b in the binary-op layout, tmp += c
-                from oracle import layout as OL
-
-                lab = OL.layout_for_binary_op((shape, stride, off), (shape, stride, off))
-                tmp = O.empty_strided(lab[0], lab[1], dt)
-                O.binary("mul", tmp, a, b, nthreads)
-                O.binary("add", tmp, tmp, cst, nthreads)
-                osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [1, 3])
-                so = O.empty_strided(osh, ost, dt)
-                O.reduce_axes("sum", a, [1, 3], so, nthreads)
-                osh, ost, _ = OL.reduce_output_layout((shape, stride, off), [3])
-                go = O.empty_strided(osh, ost, np.uint64)
-                O.argreduce_axes(True, a, [3], go, nthreads)
-                tot_t += time.perf_counter() - t0
-                tot_b += op_bytes_n(esize, kind, n, shape)
-    return tot_t, tot_b
+    tot_t, tot_b, outs = 0.0, 0, []
+    for cs in cases:
+        shape, stride, off, dt = cs["shape"], cs["stride"], cs["off"], cs["dt"]
+        n = int(np.prod(shape))
+        a = O.Strided(cs["ha"], shape, stride, off)
+        b = O.Strided(cs["hb"], shape, stride, off)
+        cst = O.Strided(cs["hc"], shape, (0, CSHAPE[3], 0, 1), 0)
+        pshape, pstride = permuted_view(shape, stride)
+        lab = OL.layout_for_binary_op((shape, stride, off), (shape, stride, off))
+        so_l = OL.reduce_output_layout((shape, stride, off), [1, 3])
+        go_l = OL.reduce_output_layout((shape, stride, off), [3])
+        res = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            dst = None
+            if cs["kind"] != "perm":
+                dst = O.empty_strided(pshape, c_stride(pshape), dt)
+                O.assign_arbitrary(dst, O.Strided(cs["ha"], pshape, pstride, off), 0, nthreads)
+            tmp = O.empty_strided(lab[0], lab[1], dt)
+            O.binary("mul", tmp, a, b, nthreads)
+            O.binary("add", tmp, tmp, cst, nthreads)
+            so = O.empty_strided(so_l[0], so_l[1], dt)
+            O.reduce_axes("sum", a, [1, 3], so, nthreads)
+            go = O.empty_strided(go_l[0], go_l[1], np.uint64)
+            O.argreduce_axes(True, a, [3], go, nthreads)
+            tot_t += time.perf_counter() - t0
+            tot_b += op_bytes_n(cs["esize"], cs["kind"], n, shape)
+            res = (dst, tmp, so, go)
+        if keep:
+            outs.append(res)
+    return tot_t, tot_b, outs
 
 
 def op_bytes_n(esize, kind, n, shape):
@@ -1098,37 +1273,79 @@ def op_bytes_n(esize, kind, n, shape):
             + n * esize + shape[0] * shape[1] * shape[2] * 8)
 
 
-def cpu_baseline(args):
+def check_outputs(wl, cases, outs):
+    """Compare the GPU outputs of the timed step (leading `batch` slabs of
+    every case) with the oracle's outputs on the same host data: copies, the
+    fused a*b+c and argmax bit-exact, sums within 1e-13 (f64) / 1e-5 (f32)
+    normwise, integers exact."""
+    bad, worst = [], {}
+    for cs, (dst, tmp, so, go) in zip(cases, outs):
+        c = next(x for x in wl.cases if x["dname"] == cs["dname"] and x["kind"] == cs["kind"])
+        lead = (slice(0, cs["shape"][0]),)
+        name = f"{cs['dname']}/{cs['kind']}"
+        if dst is not None and not np.array_equal(c["out_perm"].i(lead).to_numpy(), dst.values()):
+            bad.append(name + "/to_contig")
+        if not np.array_equal(c["d"].i(lead).to_numpy(), tmp.values()):
+            bad.append(name + "/fma")
+        got, want = c["sum_out"].i(lead).to_numpy(), so.values()
+        if np.dtype(cs["dt"]).kind == "i":
+            if not np.array_equal(got, want):
+                bad.append(name + "/sum")
+        else:
+            err = float(np.max(np.abs(got.astype(np.float64) - want)) / max(float(np.max(np.abs(want))), 1e-300))
+            worst[cs["dname"]] = max(worst.get(cs["dname"], 0.0), err)
+            if err > (1e-13 if cs["dt"] == np.float64 else 1e-5):
+                bad.append(name + "/sum")
+        if not np.array_equal(c["arg_out"].i(lead).to_numpy(), go.values()):
+            bad.append(name + "/argmax")
+    return {"ok": not bad, "mismatches": bad,
+            "checked": f"every output of the timed step on the leading {cases[0]['shape'][0]} of 32 slabs "
+                       "of every case against the oracle (copies, a*b+c, argmax and integer sums bit-exact)",
+            "sum_max_normwise_err": {k: float(f"{v:.3g}") for k, v in worst.items()}}
+
+
+def cpu_baseline(args, wl=None):
+    """The oracle on all host cores on a bounded sample of the step (the
+    leading --cpu-batch of 32 slabs, the GPU workload's own host data), its
+    operations repeated until about --cpu-seconds of CPU work is timed. With
+    the GPU workload given, the outputs of that sample also check the GPU's."""
     from oracle import oracle as O
 
     nth = O.max_threads()
-    batch = args.cpu_batch
-    t, b = cpu_sample_step(batch, nth)  # one pass sizes the repeat count
+    cases = host_cases(src=wl, batch=args.cpu_batch)
+    t, b, outs = cpu_step(cases, nth, keep=wl is not None)  # one pass sizes the repeat count
+    parity = check_outputs(wl, cases, outs) if wl is not None else None
+    del outs
     reps = max(1, min(200, math.ceil(args.cpu_seconds / max(t, 1e-3))))
     if reps > 1:
-        t, b = cpu_sample_step(batch, nth, reps=reps)
-    return {"value": round(b / t / 1e9, 2), "unit": "GB/s", "cores": nth, "kind": "port",
-            "sample": f"the step at leading extent {batch} of 32 (all dtypes and layouts), each case's operations "
-                      f"timed {reps} times: {b / 1e9:.2f} GB in {t:.2f} s"}
+        t, b, _ = cpu_step(cases, nth, reps=reps)
+    res = {"value": round(b / t / 1e9, 2), "unit": "GB/s", "cores": nth, "kind": "port",
+           "sample": f"the step at leading extent {args.cpu_batch} of 32 (all dtypes and layouts), each case's "
+                     f"operations timed {reps} times: {b / 1e9:.2f} GB in {t:.2f} s"}
+    return res, parity
 
 
 def run_reference(args):
+    """The reference arm: the OpenMP restatement of rstsr's rayon kernels on
+    every host core, on the full workload (all 32 slabs, every dtype and
+    layout); inputs generated once, each step one pass of the operations."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
     from oracle import oracle as O
 
     nth = O.max_threads()
-    batch = args.cpu_batch
+    cases = host_cases(batch=args.ref_batch)
     for _ in range(args.warmup):
-        cpu_sample_step(batch, nth)
+        cpu_step(cases, nth)
     tt, bb = 0.0, 0
     for _ in range(args.steps):
-        t, b = cpu_sample_step(batch, nth)
+        t, b, _ = cpu_step(cases, nth)
         tt += t
         bb += b
     value = bb / tt / 1e9
-    sample = f"each step: leading extent {batch} of 32, all dtypes and layouts ({bb / args.steps / 1e9:.2f} GB)"
+    what = "the full workload, all 32 slabs" if args.ref_batch == 32 else f"leading extent {args.ref_batch} of 32"
+    sample = f"each step: {what}, all dtypes and layouts ({bb / args.steps / 1e9:.2f} GB)"
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -1143,9 +1360,7 @@ def run_reference(args):
         "vs_baseline": None,
         "dtype": "f64,f32,i32",
         "data": "synthetic (seeded uniform; i32 uniform in [-1000,1000])",
-        "config": {"workload": "strided ops [32,64,128,128] x {f64,f32,i32} x {C,F,permuted,step-2 slice}: "
-                               "permute(0,2,1,3)+to_contig, a*b+c (c [1,64,1,128]), sum(1,3), argmax(-1)",
-                   "parallelism": "host cores"},
+        "config": {"workload": WORKLOAD, "parallelism": "host cores"},
         "cpu_baseline": {"value": round(value, 2), "unit": "GB/s", "cores": nth, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 2), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -1160,15 +1375,18 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-gemm", action="store_true")
-    ap.add_argument("--cpu-batch", type=int, default=4)
+    ap.add_argument("--cpu-batch", type=int, default=4, help="leading slabs of the cpu_baseline sample")
+    ap.add_argument("--ref-batch", type=int, default=32,
+                    help="leading slabs of the reference arm's step (32: the full workload)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0,
                     help="CPU work the cpu_baseline sample is sized to (the operations repeated)")
     # restrict the workload (profiling a small case): comma-separated subsets
     ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
-    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction"],
+    ap.add_argument("--rate-n", type=int, default=8192, help="matrix order for --only rates")
+    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction", "rates"],
                     help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select; "
-                         "contraction: only einsum / vecdot")
+                         "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates")
     ap.add_argument("--ein-p", type=int, default=1000, help="P of the 3-index transform for --only contraction")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
@@ -1178,6 +1396,8 @@ def main():
     args = ap.parse_args()
     if args.only == "c3":
         res = run_c3_only(args)
+    elif args.only == "rates":
+        res = run_rates(args)
     elif args.only == "tri_index":
         res = run_tri_index_only(args)
     elif args.only == "contraction":

@@ -10,7 +10,9 @@ ROOT = Path(__file__).resolve().parent.parent
 
 
 def test_reference_arm_json_line(built_lib):
-    res = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"],
+    # two leading slabs of the 32 keep this CPU test short; the default is the full workload
+    res = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3",
+                          "--ref-batch", "2"],
                          cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert res.returncode == 0, res.stderr[-2000:]
     lines = [l for l in res.stdout.splitlines() if l.strip().startswith("{")]
