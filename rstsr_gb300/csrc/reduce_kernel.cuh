@@ -175,6 +175,81 @@ struct Red<T, kRedSum> {
     }
 };
 
+// f64 sum and mean without the FP64 pipe (GB300 issues about two FP64 adds
+// per cycle and SM, which bounded the f64 sums below the memory rate). The
+// accumulator is a signed 64-bit integer S in units of 2^(E - 1075), E being
+// the largest biased exponent seen so far: a double x = +-M 2^(ex - 1075)
+// (M the 53-bit significand, ex >= 1) adds +-(M >> (E - ex)), i.e. x
+// truncated to that unit, an error below 2^-52 of the largest magnitude per
+// term (an FP64 add rounds at 2^-53 of the running sum). A larger exponent
+// shifts S right first. |S| is kept below 2^62 (one halving with E + 1 after
+// each round of at most a few hundred terms; a term is below 2^53), so S never
+// overflows. All steps are integer and deterministic. NaN and +-inf terms go
+// to an FP64 side sum, added at the end with IEEE semantics (inf + -inf = NaN).
+// The integer fold costs about 25 ALU instructions a term, so the walks hand
+// every other term to the FP64 pipe instead (fold_fp, a plain FP64 add into
+// d): the two pipes then share the work, and the result is the fixed-point
+// sum plus d, still deterministic.
+struct AccFix {
+    long long s;   // the fixed-point sum
+    int32_t e;     // biased exponent of its unit + 1075
+    int32_t nonfinite;
+    double spec;   // sum of the NaN / inf terms
+    double d;      // FP64 sum of the terms given to the FP64 pipe
+};
+template <>
+struct Red<double, kRedSum> {
+    using Acc = AccFix;
+    using Out = double;
+    __device__ static Acc init() { return {0, 1, 0, 0.0, 0.0}; }
+    __device__ static void fold_fp(Acc& a, double x) { a.d += x; }
+    __device__ static void fix(Acc& a) {
+        const long long lim = (long long)1 << 62;
+        if (a.s >= lim || a.s <= -lim) {
+            a.s >>= 1;
+            a.e += 1;
+        }
+    }
+    __device__ static void fold(Acc& a, double x, int64_t) {
+        const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+        const int ex = (int)((b >> 52) & 0x7FF);
+        if (ex == 0x7FF) {
+            a.nonfinite = 1;
+            a.spec += x;
+            return;
+        }
+        long long m = (long long)(b & 0xFFFFFFFFFFFFFULL) | (ex ? (1LL << 52) : 0LL);
+        const int exe = ex > 1 ? ex : 1;
+        if (exe > a.e) {
+            const int up = exe - a.e;
+            a.s = up > 63 ? (a.s < 0 ? -1 : 0) : (a.s >> up);
+            a.e = exe;
+        }
+        const int d = a.e - exe;
+        m = d > 63 ? 0 : (m >> d);
+        a.s += (b >> 63) ? -m : m;
+    }
+    __device__ static void merge(Acc& a, const Acc& o) {
+        if (o.nonfinite) {
+            a.nonfinite = 1;
+            a.spec += o.spec;
+        }
+        a.d += o.d;
+        const int e = a.e > o.e ? a.e : o.e;
+        const int da = e - a.e, db = e - o.e;
+        const long long sa = da > 63 ? (a.s < 0 ? -1 : 0) : (a.s >> da);
+        const long long sb = db > 63 ? (o.s < 0 ? -1 : 0) : (o.s >> db);
+        a.s = sa + sb;
+        a.e = e;
+        fix(a);
+    }
+    __device__ static Out fin(const Acc& a, int op, int64_t n) {
+        double r = ldexp((double)a.s, a.e - 1075) + a.d;
+        if (a.nonfinite) r += a.spec;
+        return op == RSTSR_RED_MEAN ? r / (double)n : r;
+    }
+};
+
 template <typename T>
 struct Red<T, kRedMoments> {
     using Acc = AccPair<T>;
@@ -278,7 +353,17 @@ struct RedLocal : Red<T, KIND> {
     __device__ static Local linit() { return R::init(); }
     __device__ static void lfold(Local& s, T x, uint32_t li) { R::fold(s, x, (int64_t)li); }
     __device__ static typename R::Acc to_acc(const Local& s) { return s; }
+    // after every round of loads: keeps the fixed-point f64 sum in range
+    __device__ static void lfix(Local& s) {
+        if constexpr (KIND == kRedSum && std::is_same<T, double>::value) R::fix(s);
+    }
+    // the f64 sum gives every other term to the FP64 pipe
+    static constexpr bool kSplitPipe = KIND == kRedSum && std::is_same<T, double>::value;
+    __device__ static void lfold_fp(Local& s, T x) {
+        if constexpr (kSplitPipe) R::fold_fp(s, x);
+    }
     static constexpr bool kArg = false;
+
     // (the ordered-walk key interface of the arg reductions; unused here)
     using Key = int;
     __device__ static Key kstart() { return 0; }
@@ -318,6 +403,9 @@ struct RedArg {
     }
     __device__ static Acc init() { return {start(), INT64_MAX, 0}; }
     __device__ static Local linit() { return {start(), UINT32_MAX}; }
+    __device__ static void lfix(Local&) {}
+    static constexpr bool kSplitPipe = false;
+    __device__ static void lfold_fp(Local&, T) {}
     template <typename I>
     __device__ static bool better(T x, I ix, T v, I iv) {
         return (IS_MAX ? (x > v) : (x < v)) | ((x == v) & (ix < iv));
@@ -371,6 +459,9 @@ struct RedArgF64 {
     // keys of non-NaN doubles lie strictly inside (INT64_MIN, INT64_MAX)
     __device__ static Acc init() { return {IS_MAX ? INT64_MIN : INT64_MAX, INT64_MAX, 0}; }
     __device__ static Local linit() { return {IS_MAX ? INT64_MIN : INT64_MAX, UINT32_MAX}; }
+    __device__ static void lfix(Local&) {}
+    static constexpr bool kSplitPipe = false;
+    __device__ static void lfold_fp(Local&, double) {}
     template <typename I>
     __device__ static bool better(int64_t x, I ix, int64_t v, I iv) {
         return (IS_MAX ? (x > v) : (x < v)) | ((x == v) & (ix < iv));
@@ -453,8 +544,18 @@ struct alignas(sizeof(T) * VEC) RVec {
 };
 
 // Input offset and logical index of row `row` of the reduced space: its dims
-// 1 .. nd-1 (dim 1 fastest); dim 0 is the column inside the row.
+// 1 .. nd-1 (dim 1 fastest); dim 0 is the column inside the row. Reduced
+// spaces of one or two dims (the common case after collapsing) read their one
+// row stride at a fixed parameter offset; deeper ones loop.
 __device__ __forceinline__ int64_t red_row_offset(const RedSpace& r, uint32_t row, uint32_t* lrow) {
+    if (r.nd <= 1) {
+        *lrow = 0;
+        return 0;
+    }
+    if (r.nd == 2) {
+        *lrow = row * (uint32_t)r.lstride[1];
+        return (int64_t)row * r.stride[1];
+    }
     int64_t off = 0;
     uint32_t li = 0;
     for (int i = 1; i < r.nd - 1; ++i) {
@@ -464,23 +565,23 @@ __device__ __forceinline__ int64_t red_row_offset(const RedSpace& r, uint32_t ro
         li += idx * (uint32_t)r.lstride[i];
         row = q;
     }
-    if (r.nd > 1) {
-        off += (int64_t)row * r.stride[r.nd - 1];
-        li += row * (uint32_t)r.lstride[r.nd - 1];
-    }
+    off += (int64_t)row * r.stride[r.nd - 1];
+    li += row * (uint32_t)r.lstride[r.nd - 1];
     *lrow = li;
     return off;
 }
 
 __device__ __forceinline__ int64_t kept_offset(const KeptSpace& k, uint32_t e, bool out) {
+    const int64_t* st = out ? k.out_stride : k.in_stride;
+    if (k.nd <= 0) return 0;
+    if (k.nd == 1) return (int64_t)e * st[0];
     int64_t off = 0;
     for (int i = 0; i < k.nd - 1; ++i) {
         const uint32_t q = k.div[i].div(e);
-        off += (int64_t)(e - q * k.shape[i]) * (out ? k.out_stride[i] : k.in_stride[i]);
+        off += (int64_t)(e - q * k.shape[i]) * st[i];
         e = q;
     }
-    if (k.nd > 0) off += (int64_t)e * (out ? k.out_stride[k.nd - 1] : k.in_stride[k.nd - 1]);
-    return off;
+    return off + (int64_t)e * st[k.nd - 1];
 }
 
 // Outputs per thread of the vectorised column regime: a 16-byte (f64: two,
@@ -558,11 +659,20 @@ __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedP
                     const bool take = R::kwins(m, best);
                     best = take ? m : best;
                     best_r = take ? lu : best_r;
+                } else if constexpr (R::kSplitPipe) {
+#pragma unroll
+                    for (int j = 0; j < W; ++j) {
+                        if ((W > 1 ? j : u) & 1)
+                            R::lfold(acc, v[u].v[j], lu + (uint32_t)j * l0);
+                        else
+                            R::lfold_fp(acc, v[u].v[j]);
+                    }
                 } else {
 #pragma unroll
                     for (int j = 0; j < W; ++j) R::lfold(acc, v[u].v[j], lu + (uint32_t)j * l0);
                 }
             }
+        R::lfix(acc);
     }
     if constexpr (kFast) {
         if (best_r != UINT32_MAX) {
@@ -627,11 +737,18 @@ __device__ __forceinline__ void red_cols(const RedParams& p, const T* __restrict
                         const bool take = R::kwins(k, acc[j].v);
                         acc[j].v = take ? k : acc[j].v;
                         acc[j].idx = take ? li[u] : acc[j].idx;
+                    } else if constexpr (R::kSplitPipe) {
+                        if (u & 1)
+                            R::lfold(acc[j], v[u].v[j], li[u]);
+                        else
+                            R::lfold_fp(acc[j], v[u].v[j]);
                     } else {
                         R::lfold(acc[j], v[u].v[j], li[u]);
                     }
                 }
             }
+#pragma unroll
+        for (int j = 0; j < OV; ++j) R::lfix(acc[j]);
     }
 }
 
@@ -765,15 +882,8 @@ __global__ void __launch_bounds__(kRedThreads) reduce_combine_kernel(const RedPa
     const Acc* part = reinterpret_cast<const Acc*>(p.partial);
     Acc acc = part[o];
     for (int s = 1; s < p.nsplit; ++s) R::merge(acc, part[(int64_t)s * p.nout + o]);
-    int64_t oo = p.out_off;
-    uint32_t e = (uint32_t)o;
-    for (int i = 0; i < p.k.nd - 1; ++i) {
-        uint32_t q = p.k.div[i].div(e);
-        oo += (int64_t)(e - q * p.k.shape[i]) * p.k.out_stride[i];
-        e = q;
-    }
-    if (p.k.nd > 0) oo += (int64_t)e * p.k.out_stride[p.k.nd - 1];
-    reinterpret_cast<typename R::Out*>(p.out)[oo] = R::fin(acc, p.op, p.nred);
+    reinterpret_cast<typename R::Out*>(p.out)[p.out_off + kept_offset(p.k, (uint32_t)o, true)] =
+        R::fin(acc, p.op, p.nred);
 }
 
 // Size of the accumulator of (T, KIND) in bytes (host side, for scratch).
