@@ -1085,6 +1085,19 @@ def run_contraction_only(args):
     return {"section": "contraction", "results": res}
 
 
+def run_batched_only(args):
+    """Only the batched / grouped GEMM section (profiling)."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    dev = rt.DeviceCuda(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev.set_stream(stream.cuda_stream)
+    return {"section": "batched", "results": run_batched_section(dev, stream)}
+
+
 def run_tri_index_only(args):
     """Only the packed-triangle / index-selection section (profiling)."""
     import torch
@@ -1384,9 +1397,9 @@ def main():
     ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
     ap.add_argument("--rate-n", type=int, default=8192, help="matrix order for --only rates")
-    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction", "rates"],
+    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction", "rates", "batched"],
                     help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select; "
-                         "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates")
+                         "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates; batched: only C5")
     ap.add_argument("--ein-p", type=int, default=1000, help="P of the 3-index transform for --only contraction")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
@@ -1398,6 +1411,8 @@ def main():
         res = run_c3_only(args)
     elif args.only == "rates":
         res = run_rates(args)
+    elif args.only == "batched":
+        res = run_batched_only(args)
     elif args.only == "tri_index":
         res = run_tri_index_only(args)
     elif args.only == "contraction":

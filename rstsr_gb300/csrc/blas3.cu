@@ -26,30 +26,80 @@ namespace {
 constexpr int kTrsmBlock = 64;
 
 // X := T^{-1} X for a kTrsmBlock-or-smaller triangular block T (lower: forward
-// substitution, upper: backward), X the block's rows of B, one thread per column.
+// substitution, upper: backward), X the block's rows of B, in the
+// right-looking order: once x_q is final every later row subtracts
+// T[i][q] x_q. Four threads share a column, thread k holding rows
+// i = 4 j + k (j < 16) in registers (a cyclic split: each does a quarter of
+// the updates at every step); the owner of row q scales it by the diagonal's
+// reciprocal and a shuffle hands x_q to the other three. T sits transposed in
+// shared memory (a quad's four rows of one column are neighbours: no bank
+// conflicts), padded to an identity triangle when nb < 64. Measured on GB300:
+// a warp issues FP64 at one SM sub-partition's share, so one thread per
+// column (32 warps for 1024 columns) left the FP64 units 85 % idle and a
+// 64-row leaf took 105 us; an earlier kernel also re-read every solved entry
+// from global memory inside a left-looking loop (leaves 72 % of a 4096 TRSM).
+constexpr int kTrsmLanes = 4;                          // threads per column
+constexpr int kTrsmRowsPerLane = kTrsmBlock / kTrsmLanes;
+constexpr int kTrsmLeafThreads = 128;
+
 template <typename T>
-__global__ void __launch_bounds__(256) trsm_diag_kernel(const T* __restrict__ a, int64_t a_si, int64_t a_sj,
-                                                        T* __restrict__ b, int64_t b_si, int64_t b_sj, int nb,
-                                                        int64_t ncols, int lower, int unit) {
-    __shared__ T tile[kTrsmBlock][kTrsmBlock + 1];
-    for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-        const int i = idx / nb, j = idx % nb;
-        tile[i][j] = a[i * a_si + j * a_sj];
+__global__ void __launch_bounds__(kTrsmLeafThreads) trsm_diag_kernel(const T* __restrict__ a, int64_t a_si,
+                                                                     int64_t a_sj, T* __restrict__ b, int64_t b_si,
+                                                                     int64_t b_sj, int nb, int64_t ncols, int lower,
+                                                                     int unit) {
+    __shared__ T tt[kTrsmBlock][kTrsmBlock];  // tt[q][i] = T[i][q]
+    __shared__ T rdiag[kTrsmBlock];
+    for (int idx = threadIdx.x; idx < kTrsmBlock * kTrsmBlock; idx += blockDim.x) {
+        const int i = idx / kTrsmBlock, q = idx % kTrsmBlock;
+        tt[q][i] = (i < nb && q < nb) ? a[i * a_si + q * a_sj] : (i == q ? (T)1 : (T)0);
     }
     __syncthreads();
-    const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= ncols) return;
-    T* x = b + col * b_sj;
-    for (int s = 0; s < nb; ++s) {
-        const int i = lower ? s : nb - 1 - s;
-        T acc = x[i * b_si];
-        if (lower) {
-            for (int p = 0; p < i; ++p) acc -= tile[i][p] * x[p * b_si];
-        } else {
-            for (int p = i + 1; p < nb; ++p) acc -= tile[i][p] * x[p * b_si];
+    for (int i = threadIdx.x; i < kTrsmBlock; i += blockDim.x) rdiag[i] = unit ? (T)1 : (T)1 / tt[i][i];
+    __syncthreads();
+    const int k = threadIdx.x & (kTrsmLanes - 1);
+    const int64_t col = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / kTrsmLanes;
+    const bool live = col < ncols;  // every lane stays for the shuffles
+    T* xc = b + (live ? col : 0) * b_sj;
+    const int lead = (threadIdx.x & 31) & ~(kTrsmLanes - 1);
+    T x[kTrsmRowsPerLane];
+#pragma unroll
+    for (int j = 0; j < kTrsmRowsPerLane; ++j) {
+        const int i = kTrsmLanes * j + k;
+        x[j] = (live && i < nb) ? xc[i * b_si] : (T)0;
+    }
+    if (lower) {
+#pragma unroll
+        for (int q = 0; q < kTrsmBlock; ++q) {
+            const int jq = q / kTrsmLanes;
+            const T xq = __shfl_sync(0xffffffffu, x[jq] * rdiag[q], lead | (q % kTrsmLanes));
+            if (k == q % kTrsmLanes) x[jq] = xq;
+#pragma unroll
+            for (int j = 0; j < kTrsmRowsPerLane; ++j) {
+                const int i0 = kTrsmLanes * j;  // this slot's rows are i0 .. i0 + 3
+                if (i0 + kTrsmLanes - 1 <= q) continue;
+                if (i0 > q || i0 + k > q) x[j] -= tt[q][i0 + k] * xq;
+            }
         }
-        if (!unit) acc = acc / tile[i][i];
-        x[i * b_si] = acc;
+    } else {
+#pragma unroll
+        for (int q = kTrsmBlock - 1; q >= 0; --q) {
+            const int jq = q / kTrsmLanes;
+            const T xq = __shfl_sync(0xffffffffu, x[jq] * rdiag[q], lead | (q % kTrsmLanes));
+            if (k == q % kTrsmLanes) x[jq] = xq;
+#pragma unroll
+            for (int j = 0; j < kTrsmRowsPerLane; ++j) {
+                const int i0 = kTrsmLanes * j;
+                if (i0 >= q) continue;
+                if (i0 + kTrsmLanes - 1 < q || i0 + k < q) x[j] -= tt[q][i0 + k] * xq;
+            }
+        }
+    }
+    if (live) {
+#pragma unroll
+        for (int j = 0; j < kTrsmRowsPerLane; ++j) {
+            const int i = kTrsmLanes * j + k;
+            if (i < nb) xc[i * b_si] = x[j];
+        }
     }
 }
 
@@ -271,13 +321,14 @@ int rstsr_cuda_trsm(rstsr_ctx* ctx, rstsr_order order, char side, char uplo, cha
     // more efficiently than many K = kTrsmBlock updates.
     auto solve_block = [&](int64_t r0, int64_t r1) -> int {
         const Layout Ad = sub_view(A, r0, r1, r0, r1), Bd = sub_view(B, r0, r1, 0, cols);
-        const unsigned grid = (unsigned)((cols + 255) / 256);
+        const int64_t threads = cols * kTrsmLanes;
+        const unsigned grid = (unsigned)((threads + kTrsmLeafThreads - 1) / kTrsmLeafThreads);
         if (t == RSTSR_F64)
-            trsm_diag_kernel<double><<<grid, 256, 0, ctx->stream>>>(
+            trsm_diag_kernel<double><<<grid, kTrsmLeafThreads, 0, ctx->stream>>>(
                 (const double*)a + Ad.offset, Ad.stride[0], Ad.stride[1], (double*)b + Bd.offset, Bd.stride[0],
                 Bd.stride[1], (int)(r1 - r0), cols, lower ? 1 : 0, unit ? 1 : 0);
         else
-            trsm_diag_kernel<float><<<grid, 256, 0, ctx->stream>>>(
+            trsm_diag_kernel<float><<<grid, kTrsmLeafThreads, 0, ctx->stream>>>(
                 (const float*)a + Ad.offset, Ad.stride[0], Ad.stride[1], (float*)b + Bd.offset, Bd.stride[0],
                 Bd.stride[1], (int)(r1 - r0), cols, lower ? 1 : 0, unit ? 1 : 0);
         return after_launch(ctx, "trsm_diag_kernel");
