@@ -1085,6 +1085,35 @@ def run_contraction_only(args):
     return {"section": "contraction", "results": res}
 
 
+def run_trsm_only(args):
+    """Only TRSM (profiling): lower triangle L = tril(N(0, 0.02)) + 2 I of order
+    --trsm-n, n right-hand sides B ~ N(0, 1), seed 0; each call copies B into
+    the work matrix and solves L X = B in place; CUDA events over --steps calls."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    dev = rt.DeviceCuda(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev.set_stream(stream.cuda_stream)
+    n = args.trsm_n
+    rng = np.random.default_rng(0)
+    L = np.tril(rng.standard_normal((n, n)) * 0.02) + np.eye(n) * 2.0
+    B = rng.standard_normal((n, n))
+    tL, tB = rt.asarray(L, dev), rt.asarray(B, dev)
+    work = rt.empty((n, n), np.float64, dev)
+
+    def solve():
+        rt.assign(work, tB)
+        rt.trsm(tL, work, "L", "L", "N", "N")
+
+    for _ in range(max(args.warmup - 1, 0)):
+        solve()
+    sec = _time_events(stream, solve, max(args.steps, 1))
+    return {"section": "trsm", "n": n, "ms": round(sec * 1e3, 3), "tflops": round(float(n) ** 3 / sec / 1e12, 2)}
+
+
 def run_batched_only(args):
     """Only the batched / grouped GEMM section (profiling)."""
     import torch
@@ -1397,9 +1426,10 @@ def main():
     ap.add_argument("--dtypes", default="", help="subset of f64,f32,i32")
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
     ap.add_argument("--rate-n", type=int, default=8192, help="matrix order for --only rates")
-    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction", "rates", "batched"],
+    ap.add_argument("--trsm-n", type=int, default=4096, help="order (and right-hand sides) for --only trsm")
+    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction", "rates", "batched", "trsm"],
                     help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select; "
-                         "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates; batched: only C5")
+                         "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates; batched: only C5; trsm: only TRSM")
     ap.add_argument("--ein-p", type=int, default=1000, help="P of the 3-index transform for --only contraction")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
@@ -1413,6 +1443,8 @@ def main():
         res = run_rates(args)
     elif args.only == "batched":
         res = run_batched_only(args)
+    elif args.only == "trsm":
+        res = run_trsm_only(args)
     elif args.only == "tri_index":
         res = run_tri_index_only(args)
     elif args.only == "contraction":
