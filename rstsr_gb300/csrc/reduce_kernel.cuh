@@ -872,16 +872,40 @@ cudaError_t launch_reduce_pass(const RedParams& p, dim3 grid, cudaStream_t strea
     return cudaGetLastError();
 }
 
-// Fold the per-chunk accumulators of every output in chunk order.
+// Fold the per-chunk accumulators of every output: a CTA takes 32 outputs,
+// its 8 warps each fold the chunks s = w, w + 8, ... of those outputs (loads
+// coalesced across the outputs, four in flight), and the 8 partial folds are
+// merged in warp order. The order is fixed by the launch shape, so results
+// are deterministic. One thread per output folding every chunk in sequence
+// was latency-bound: 16 us for the 152 chunks of 4096 outputs (an F-ordered
+// f32 sum over two axes), 39 % of that reduction.
+constexpr int kCombOuts = 32, kCombLanes = kRedThreads / kCombOuts;
+
 template <typename T, int KIND>
 __global__ void __launch_bounds__(kRedThreads) reduce_combine_kernel(const RedParams p) {
     using R = Red<T, KIND>;
     using Acc = typename R::Acc;
-    const int64_t o = (int64_t)blockIdx.x * kRedThreads + threadIdx.x;
-    if (o >= p.nout) return;
+    __shared__ Acc part_acc[kCombLanes][kCombOuts];
+    const int ol = threadIdx.x % kCombOuts, sl = threadIdx.x / kCombOuts;
+    const int64_t o = (int64_t)blockIdx.x * kCombOuts + ol;
     const Acc* part = reinterpret_cast<const Acc*>(p.partial);
-    Acc acc = part[o];
-    for (int s = 1; s < p.nsplit; ++s) R::merge(acc, part[(int64_t)s * p.nout + o]);
+    Acc acc = R::init();
+    if (o < p.nout) {
+        int s = sl;
+        for (; s + 3 * kCombLanes < p.nsplit; s += 4 * kCombLanes) {
+            Acc v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = part[(int64_t)(s + u * kCombLanes) * p.nout + o];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) R::merge(acc, v[u]);
+        }
+        for (; s < p.nsplit; s += kCombLanes) R::merge(acc, part[(int64_t)s * p.nout + o]);
+    }
+    part_acc[sl][ol] = acc;
+    __syncthreads();
+    if (sl != 0 || o >= p.nout) return;
+#pragma unroll
+    for (int i = 1; i < kCombLanes; ++i) R::merge(acc, part_acc[i][ol]);
     reinterpret_cast<typename R::Out*>(p.out)[p.out_off + kept_offset(p.k, (uint32_t)o, true)] =
         R::fin(acc, p.op, p.nred);
 }
@@ -910,7 +934,7 @@ int launch_reduce(rstsr_ctx* ctx, RedParams p) {
     cudaError_t e = launch_reduce_pass<T, KIND>(p, dim3((unsigned)gx, (unsigned)p.nsplit), ctx->stream);
     int s = e == cudaSuccess ? after_launch(ctx, "reduce pass") : cuda_fail(e, "reduce pass");
     if (s == RSTSR_OK && p.nsplit > 1) {
-        const int64_t gc = (p.nout + kRedThreads - 1) / kRedThreads;
+        const int64_t gc = (p.nout + kCombOuts - 1) / kCombOuts;
         reduce_combine_kernel<T, KIND><<<(unsigned)gc, kRedThreads, 0, ctx->stream>>>(p);
         s = after_launch(ctx, "reduce_combine_kernel");
     }

@@ -85,7 +85,7 @@ static int launch_sum_noalloc(cudaStream_t stream, RedParams p, void* scratch) {
     cudaError_t e = launch_reduce_pass<T, kRedSum>(p, dim3((unsigned)gx, (unsigned)p.nsplit), stream);
     if (e != cudaSuccess) return cuda_fail(e, "reduce pass");
     if (p.nsplit > 1) {
-        const int64_t gc = (p.nout + kRedThreads - 1) / kRedThreads;
+        const int64_t gc = (p.nout + kCombOuts - 1) / kCombOuts;
         reduce_combine_kernel<T, kRedSum><<<(unsigned)gc, kRedThreads, 0, stream>>>(p);
         e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_fail(e, "reduce_combine_kernel");
