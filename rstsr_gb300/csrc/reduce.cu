@@ -224,7 +224,8 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         // flight; a warp's accesses stay whole 64-128-byte pieces of each
         // run), long runs about 32 (four rounds: a CTA that issues only one
         // round spends most of its life waiting for it); G <= 256
-        const int64_t W = p.r.stride[0] == 1 && (p.r.shape[0] % VEC) == 0 ? VEC : 1;
+        const bool s2_shape = VEC >= 4 && p.r.stride[0] == 2 && (p.r.shape[0] % (VEC / 2)) == 0;
+        const int64_t W = p.r.stride[0] == 1 && (p.r.shape[0] % VEC) == 0 ? VEC : s2_shape ? VEC / 2 : 1;
         const int64_t nvec = (p.nred + W - 1) / W;
         const int64_t per_lane = nvec <= 1024 ? 8 : 32;
         int G = 1, glog = 0;
@@ -255,8 +256,23 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         for (int i = 1; vec && i < p.r.nd; ++i) vec = (std::llabs(p.r.stride[i]) * (int64_t)es) % vb == 0;
         for (int i = 0; vec && i < p.k.nd; ++i) vec = (std::llabs(p.k.in_stride[i]) * (int64_t)es) % vb == 0;
         p.vec = vec ? 1 : 0;
+        // step-2 rows of 4-byte or smaller elements: 16-byte loads of which
+        // every other element is used (the other half of each sector is read
+        // anyway), aligned like the contiguous case; no negative strides, so
+        // that the view's largest offset bounds every load
+        bool s2 = !vec && s2_shape && (p.chunk % VEC) == 0 &&
+                  ((reinterpret_cast<uintptr_t>(a) + (uintptr_t)(La.offset * (int64_t)es)) % vb) == 0;
+        for (int i = 1; s2 && i < p.r.nd; ++i) s2 = p.r.stride[i] > 0 && (p.r.stride[i] * (int64_t)es) % vb == 0;
+        for (int i = 0; s2 && i < p.k.nd; ++i) s2 = p.k.in_stride[i] > 0 && (p.k.in_stride[i] * (int64_t)es) % vb == 0;
+        if (s2) {
+            int64_t mx = La.offset;
+            for (int i = 0; i < La.ndim; ++i)
+                if (La.shape[i] > 0) mx += (La.shape[i] - 1) * std::max<int64_t>(La.stride[i], 0);
+            p.max_off = mx;
+        }
+        p.s2 = s2 ? 1 : 0;
         // the group's step over the reduced elements as (rows, columns) of dim 0
-        const uint32_t step = (uint32_t)G * (uint32_t)(vec ? VEC : 1);
+        const uint32_t step = (uint32_t)G * (uint32_t)(vec ? VEC : s2 ? VEC / 2 : 1);
         p.adv_row = step / p.r.shape[0];
         p.adv_c = step % p.r.shape[0];
     } else {

@@ -80,6 +80,8 @@ struct RedParams {
     uint32_t adv_row, adv_c;
     int32_t row;   // row regime (G threads per output, G may be 1)
     int32_t mono;  // the flattened reduced index is the logical index (walks visit it in order)
+    int32_t s2;    // row regime, reduced dim 0 of stride 2: 16-byte loads serve VEC / 2 elements
+    int64_t max_off;  // largest element offset of the input view (the s2 loads stay at or below it)
     void* partial;   // [nsplit][nout] accumulators, or null
     const void* in;
     void* out;
@@ -603,7 +605,29 @@ __host__ __device__ inline int64_t red_outputs_per_cta(const RedParams& p) {
 // position advances by the host-computed (adv_row, adv_c), so a step costs an
 // add and a compare, plus the row's offset (one multiply for a 2-dim reduced
 // space, a division chain beyond), instead of a full index decomposition.
-template <typename T, int KIND, int W, bool MONO>
+// SS = 2: reduced dim 0 has stride 2 (a step-2 slice); a 16-byte load of 2W
+// raw elements serves the W elements at its even positions, and a load that
+// would reach past the view's last element (p.max_off) is replaced by W
+// scalar loads: every access stays inside the view's span.
+template <typename T, int W, int SS>
+__device__ __forceinline__ RVec<T, W> red_load(const RedParams& p, const T* __restrict__ in, int64_t at) {
+    if constexpr (SS == 1) {
+        return *reinterpret_cast<const RVec<T, W>*>(in + at);
+    } else {
+        RVec<T, W> v;
+        if (at + 2 * W - 1 <= p.max_off) {
+            const RVec<T, 2 * W> raw = *reinterpret_cast<const RVec<T, 2 * W>*>(in + at);
+#pragma unroll
+            for (int j = 0; j < W; ++j) v.v[j] = raw.v[2 * j];
+        } else {
+#pragma unroll
+            for (int j = 0; j < W; ++j) v.v[j] = in[at + 2 * j];
+        }
+        return v;
+    }
+}
+
+template <typename T, int KIND, int W, bool MONO, int SS = 1>
 __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedParams& p, const T* __restrict__ in,
                                                                    int64_t base, int lane, int G) {
     using R = RedLocal<T, KIND>;
@@ -638,7 +662,7 @@ __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedP
                 uint32_t lrow;
                 const int64_t off = red_row_offset(p.r, row, &lrow) + (int64_t)c * s0;
                 if constexpr (kKeepLi) li[u] = lrow + c * l0;
-                v[u] = *reinterpret_cast<const RVec<T, W>*>(in + base + off);
+                v[u] = red_load<T, W, SS>(p, in, base + off);
             }
             c += p.adv_c;
             row += p.adv_row;
@@ -681,7 +705,7 @@ __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedP
             const uint32_t brow = p.r.div[0].div(best_r);
             uint32_t lrow;
             const int64_t boff = red_row_offset(p.r, brow, &lrow) + (int64_t)(best_r - brow * n0) * s0;
-            const RVec<T, W> w = *reinterpret_cast<const RVec<T, W>*>(in + base + boff);
+            const RVec<T, W> w = red_load<T, W, SS>(p, in, base + boff);
             int jj = W - 1;
 #pragma unroll
             for (int j = W - 1; j >= 0; --j) jj = R::key(w.v[j]) == best ? j : jj;
@@ -799,7 +823,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_col_kernel(const RedParams
 }
 
 // Row regime: a group of G = 2^glog threads per output (G may be 1).
-template <typename T, int KIND, int W, bool MONO>
+template <typename T, int KIND, int W, bool MONO, int SS = 1>
 __global__ void __launch_bounds__(kRedThreads) reduce_row_kernel(const RedParams p) {
     using R = RedLocal<T, KIND>;
     using Acc = typename R::Acc;
@@ -813,7 +837,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_row_kernel(const RedParams
     Acc acc = R::init();
     if (active) {
         base = p.in_off + kept_offset(p.k, (uint32_t)o, false);
-        acc = R::to_acc(red_rows<T, KIND, W, MONO>(p, in, base, lane, G));
+        acc = R::to_acc(red_rows<T, KIND, W, MONO, SS>(p, in, base, lane, G));
     }
     // combine the group (fixed tree: deterministic)
     const int width = G < 32 ? G : 32;
@@ -847,6 +871,15 @@ cudaError_t launch_reduce_pass(const RedParams& p, dim3 grid, cudaStream_t strea
     constexpr bool kArg = RedLocal<T, KIND>::kArg;
     const bool mono = kArg && p.mono;
     if (p.row) {
+        if constexpr (VEC >= 4) {
+            if (p.s2) {
+                if (mono)
+                    reduce_row_kernel<T, KIND, VEC / 2, kArg, 2><<<grid, kRedThreads, 0, stream>>>(p);
+                else
+                    reduce_row_kernel<T, KIND, VEC / 2, false, 2><<<grid, kRedThreads, 0, stream>>>(p);
+                return cudaGetLastError();
+            }
+        }
         if (VEC > 1 && p.vec) {
             if (mono)
                 reduce_row_kernel<T, KIND, VEC, kArg><<<grid, kRedThreads, 0, stream>>>(p);

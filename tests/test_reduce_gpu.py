@@ -254,3 +254,26 @@ def test_f64_sum_wide_range_and_specials(dev):
     gz = rt.asarray(z, dev).sum_axes(0).to_numpy()
     wz = np.array([float(sum(map(__import__("fractions").Fraction, z[:, j]))) for j in range(6)])
     assert np.all(np.abs(gz - wz) <= 1e-13 * np.max(np.abs(z), axis=0))
+
+
+@pytest.mark.parametrize("n", [4, 6, 96, 4096])
+@pytest.mark.parametrize("dtype", [np.float32, np.int32, np.float64])
+def test_step2_rows_reaching_the_buffer_end(dev, n, dtype):
+    """Rows of a step-2 view whose last element is the last element of its
+    buffer (no element after it): the 16-byte loads of the step-2 walk stop
+    at the view's end. Against the oracle."""
+    R = 5
+    buf = rand((R * 2 * n - 1,), dtype, seed=n)
+    if np.dtype(dtype).kind == "i":
+        buf[:] = buf % 13
+    case = (buf, (R, n), (2 * n, 2), 0)
+    t = up(dev, *case)
+    for op in ("sum", "max"):
+        want, lo = oracle_reduce(op, case, [1], dtype)
+        got = rt.reduce_axes(op, t, [1])
+        assert (got.shape, got.stride) == lo
+        check_close(got.to_numpy(), want, dtype, op)
+    for is_max in (True, False):
+        out = O.empty_strided((R,), (1,), np.uint64)
+        O.argreduce_axes(is_max, O.Strided(*case), [1], out, nthreads=4)
+        np.testing.assert_array_equal(rt.argreduce_axes(is_max, t, [1]).to_numpy(), out.values())
