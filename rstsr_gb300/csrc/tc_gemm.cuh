@@ -585,7 +585,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const TcGemmPara
                     for (int kt = c0; kt < c1; ++kt, ++it) {
                         const uint32_t s = it % stages;
                         const uint32_t ph = (it / stages) & 1u;
-                        if (!tc::mbar_wait(&full[s], ph)) {
+                        if (!tc::mbar_wait_spin(&full[s], ph)) {
                             atomicExch(p.err, kTcErrMmaWait);
                             *abort_flag = 1;
                         }
