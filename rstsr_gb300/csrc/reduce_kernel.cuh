@@ -631,6 +631,9 @@ template <typename T, int KIND, int W, bool MONO, int SS = 1>
 __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedParams& p, const T* __restrict__ in,
                                                                    int64_t base, int lane, int G) {
     using R = RedLocal<T, KIND>;
+    // 8-byte elements: four loads in flight (their accumulators and keys take
+    // twice the registers)
+    constexpr int U = sizeof(T) >= 8 ? kRedUnroll / 2 : kRedUnroll;
     typename R::Local acc = R::linit();
     const int64_t rb = (int64_t)blockIdx.y * p.chunk;
     const int64_t re = min(p.nred, rb + p.chunk);
@@ -654,10 +657,10 @@ __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedP
     constexpr bool kKeepLi = R::kArg && !MONO;
     for (; r < re;) {
         const int64_t r0 = r;
-        RVec<T, W> v[kRedUnroll];
-        [[maybe_unused]] uint32_t li[kKeepLi ? kRedUnroll : 1];
+        RVec<T, W> v[U];
+        [[maybe_unused]] uint32_t li[kKeepLi ? U : 1];
 #pragma unroll
-        for (int u = 0; u < kRedUnroll; ++u) {
+        for (int u = 0; u < U; ++u) {
             if (r0 + u * step < re) {
                 uint32_t lrow;
                 const int64_t off = red_row_offset(p.r, row, &lrow) + (int64_t)c * s0;
@@ -671,9 +674,9 @@ __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedP
                 ++row;
             }
         }
-        r = r0 + kRedUnroll * step;
+        r = r0 + U * step;
 #pragma unroll
-        for (int u = 0; u < kRedUnroll; ++u)
+        for (int u = 0; u < U; ++u)
             if (r0 + u * step < re) {
                 const uint32_t lu = kKeepLi ? li[kKeepLi ? u : 0] : (uint32_t)(r0 + u * step);
                 if constexpr (kFast) {
