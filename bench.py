@@ -430,7 +430,9 @@ def gemm_summary(g, small):
                  "bcast_tflops": bc["tflops"], "bcast_err": float(f"{bc['rel_err_frobenius']:.3g}"),
                  "graph_us": ch["graph_us_per_iter"], "eager_us": ch["eager_us_per_iter"]}
     out["c1_small_f64"] = {"exact_add": small["add_bit_exact"], "exact_argmax": small["argmax_exact"],
-                           "matmul_err": float(f"{small['matmul_rel_err']:.3g}")}
+                           "matmul_err": float(f"{small['matmul_rel_err']:.3g}"),
+                           "eager_us": [small["add_us"], small["sum_axes_us"], small["argmax_axes_us"], small["matmul_us"]],
+                           "graph_4ops_us": small["graph_4ops_us"]}
     out["c3_ozaki_f64"] = {
         "tflops": c3["tflops"], "ms": c3["ms"], "slices": c3["slices"],
         "rel_err": float(f"{c3['rel_err_frobenius']:.3g}"),
@@ -835,6 +837,35 @@ def run_batched_section(dev, stream):
     return out
 
 
+def capture_small_ops(dev, tA, tb, tB):
+    """Capture C = A + b, sum_axes(C, 1), argmax_axes(C, 1) and A % B into
+    caller-owned outputs as one CUDA graph. Returns the graph and the outputs
+    (C, sums, argmax indices, product)."""
+    import rstsr_gb300 as rt
+    from rstsr_gb300 import _lib
+    from rstsr_gb300.tensor import broadcast_layouts
+
+    la, lb = broadcast_layouts(tA, tb, dev.default_order)
+    cbuf = rt.empty((tA.shape[0], tA.shape[1]), np.float64, dev)
+    s_out = rt.empty((tA.shape[0],), np.float64, dev)
+    g_out = rt.empty((tA.shape[0],), np.uint64, dev)
+    m_out = rt.empty((tA.shape[0], tB.shape[1]), np.float64, dev)
+    ax = (C.c_int64 * 1)(1)
+
+    def ops():
+        _lib.call("rstsr_cuda_binary", dev.ctx, _lib.OP["add"], cbuf.dtype_code, C.c_void_p(cbuf.ptr),
+                  C.byref(cbuf.layout()), C.c_void_p(tA.ptr), C.byref(la), C.c_void_p(tb.ptr), C.byref(lb))
+        rt.reduce_axes_into("sum", cbuf, [1], s_out)
+        _lib.call("rstsr_cuda_argreduce_axes_into", dev.ctx, 1, cbuf.dtype_code, C.c_void_p(cbuf.ptr),
+                  C.byref(cbuf.layout()), ax, 1, C.c_void_p(g_out.ptr), C.byref(g_out.layout()))
+        rt.matmul_into(m_out, tA, tB)
+
+    ops()  # first call outside the capture: workspaces are sized here
+    with rt.Graph(dev) as g:
+        ops()
+    return g, (cbuf, s_out, g_out, m_out)
+
+
 def run_small_section(dev, stream):
     """The small f64 row-major case: A [64,128] and b [128] uniform(-1,1),
     B [128,96]; C = A + b, sum_axes(C, 1), argmax_axes(C, 1), A % B. Device
@@ -851,7 +882,7 @@ def run_small_section(dev, stream):
     res["add_us"] = round(_time_events(stream, lambda: tA + tb, 200) * 1e6, 2)
     res["sum_axes_us"] = round(_time_events(stream, lambda: Cd.sum_axes(1), 200) * 1e6, 2)
     res["argmax_axes_us"] = round(_time_events(stream, lambda: Cd.argmax_axes(1), 200) * 1e6, 2)
-    res["matmul_us"] = round(_time_events(stream, lambda: rt.matmul(tA, tB, slices=7), 50) * 1e6, 2)
+    res["matmul_us"] = round(_time_events(stream, lambda: rt.matmul(tA, tB), 50) * 1e6, 2)
     C = A + b
     res["add_bit_exact"] = bool(np.array_equal(Cd.to_numpy(), C))
     s = Cd.sum_axes(1).to_numpy()
@@ -859,6 +890,15 @@ def run_small_section(dev, stream):
     res["argmax_exact"] = bool(np.array_equal(Cd.argmax_axes(1).to_numpy(), np.argmax(C, axis=1)))
     m = rt.matmul(tA, tB).to_numpy()
     res["matmul_rel_err"] = float(np.linalg.norm(m - A @ B) / np.linalg.norm(A @ B))
+    # the same four operations into caller-owned outputs, captured once as a
+    # CUDA graph and replayed: the device time of the library's launches
+    # without the Python / ctypes call overhead of the eager figures above
+    g, outs = capture_small_ops(dev, tA, tb, tB)
+    g.launch()
+    res["graph_4ops_us"] = round(_time_events(stream, g.launch, 200) * 1e6, 2)
+    cbuf, _, g_out, _ = outs
+    res["graph_bit_exact"] = bool(np.array_equal(cbuf.to_numpy(), C)) and bool(
+        np.array_equal(g_out.to_numpy(), np.argmax(C, axis=1)))
     return res
 
 
@@ -1112,6 +1152,73 @@ def run_trsm_only(args):
         solve()
     sec = _time_events(stream, solve, max(args.steps, 1))
     return {"section": "trsm", "n": n, "ms": round(sec * 1e3, 3), "tflops": round(float(n) ** 3 / sec / 1e12, 2)}
+
+
+def run_per_case_only(args):
+    """Per-case device time of every operation of the strided workload (each
+    call timed alone with CUDA events, the cases cycled so that every input is
+    cold: 268 MB f64 / 134 MB f32 operands, nine rounds, median), as a fraction
+    of the measured HBM copy rate; and torch's own reductions and copy on
+    C-contiguous inputs of the same bytes for comparison."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    dev = rt.DeviceCuda(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev.set_stream(stream.cuda_stream)
+    try:
+        peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        peak = 6800.0
+    dts = [d for d in args.dtypes.split(",") if d] or None
+    lays = [x for x in args.layouts.split(",") if x] or None
+    wl = Workload(dev, rt.lib(), seed=0, dtypes=dts, layouts=lays)
+    ops = ("to_contig", "fma", "sum", "argmax")
+    for c in wl.cases:
+        for op in ops:
+            wl.run_op(c, op)
+    torch.cuda.synchronize()
+    ev = {}
+    for _ in range(9):
+        for op in ops:
+            for c in wl.cases:
+                if not c["bytes"][op]:
+                    continue
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                wl.run_op(c, op)
+                e1.record(stream)
+                ev.setdefault((c["dname"], c["kind"], op), []).append((e0, e1))
+    torch.cuda.synchronize()
+    cases = {}
+    for (d, k, op), pairs in sorted(ev.items()):
+        ms = sorted(a.elapsed_time(b) for a, b in pairs)[len(pairs) // 2]
+        c = next(x for x in wl.cases if x["dname"] == d and x["kind"] == k)
+        cases[f"{d}/{k}/{op}"] = {"us": round(ms * 1e3, 1),
+                                  "frac_hbm": round(c["bytes"][op] / (ms * 1e-3) / 1e9 / peak, 3)}
+    del wl
+    torch_res = {}
+    for dname, dt in DTYPES:
+        if dts and dname not in dts:
+            continue
+        tdt = {"f64": torch.float64, "f32": torch.float32, "i32": torch.int32}[dname]
+        if tdt.is_floating_point:
+            x = torch.rand(N, device="cuda", dtype=tdt) * 2 - 1
+        else:
+            x = torch.randint(-1000, 1001, (N,), device="cuda", dtype=tdt)
+        nb = N * x.element_size()
+        calls = {"sum(1,3)": (lambda: x.view(SHAPE).sum(dim=(1, 3)), nb),
+                 "argmax(-1)": (lambda: x.view(SHAPE).argmax(dim=-1), nb),
+                 "copy": (lambda: x.clone(), 2 * nb)}
+        for name, (fn, b) in calls.items():
+            for _ in range(3):
+                fn()
+            sec = _time_events(stream, fn, 9)
+            torch_res[f"{dname}/c/{name}"] = {"us": round(sec * 1e6, 1), "frac_hbm": round(b / sec / 1e9 / peak, 3)}
+        del x
+    return {"section": "per_case", "peak_gbs": peak, "cases": cases, "torch": torch_res}
 
 
 def run_batched_only(args):
@@ -1427,9 +1534,12 @@ def main():
     ap.add_argument("--layouts", default="", help="subset of c,f,perm,slice")
     ap.add_argument("--rate-n", type=int, default=8192, help="matrix order for --only rates")
     ap.add_argument("--trsm-n", type=int, default=4096, help="order (and right-hand sides) for --only trsm")
-    ap.add_argument("--only", default="", choices=["", "c3", "tri_index", "contraction", "rates", "batched", "trsm"],
+    ap.add_argument("--only", default="",
+                    choices=["", "c3", "tri_index", "contraction", "rates", "batched", "trsm", "per_case"],
                     help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select; "
-                         "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates; batched: only C5; trsm: only TRSM")
+                         "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates; batched: only C5; "
+                         "trsm: only TRSM; per_case: each operation of the strided workload per (dtype, layout), "
+                         "with torch's reductions on the same bytes")
     ap.add_argument("--ein-p", type=int, default=1000, help="P of the 3-index transform for --only contraction")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
@@ -1445,6 +1555,8 @@ def main():
         res = run_batched_only(args)
     elif args.only == "trsm":
         res = run_trsm_only(args)
+    elif args.only == "per_case":
+        res = run_per_case_only(args)
     elif args.only == "tri_index":
         res = run_tri_index_only(args)
     elif args.only == "contraction":

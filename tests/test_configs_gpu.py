@@ -80,6 +80,31 @@ def test_small_f64_seed0(dev):
     assert frob(m.to_numpy(), A @ B) <= 1e-13
 
 
+def test_small_f64_graph_replayed(dev):
+    """The same four operations captured into one CUDA graph (the benchmark's
+    replayed latency figure) and replayed twice into caller-owned outputs."""
+    rng = np.random.default_rng(0)
+    A = rng.uniform(-1, 1, (64, 128))
+    b = rng.uniform(-1, 1, (128,))
+    B = rng.uniform(-1, 1, (128, 96))
+    tA, tb, tB = rt.asarray(A, dev), rt.asarray(b, dev), rt.asarray(B, dev)
+    g, (cbuf, s_out, g_out, m_out) = bench.capture_small_ops(dev, tA, tb, tB)
+    for t in (cbuf, s_out, m_out):
+        rt.fill(t, 0.0)
+    rt.fill(g_out, 7)
+    g.launch()
+    g.launch()
+    Cv = A + b
+    np.testing.assert_array_equal(cbuf.to_numpy(), Cv)
+    sref = O.empty_strided((64,), (1,), np.float64)
+    O.reduce_axes("sum", O.Strided(Cv.ravel(), (64, 128), (128, 1)), [1], sref)
+    assert normwise(s_out.to_numpy(), sref.values()) <= F64_SUM_TOL
+    gref = O.empty_strided((64,), (1,), np.uint64)
+    O.argreduce_axes(True, O.Strided(Cv.ravel(), (64, 128), (128, 1)), [1], gref)
+    np.testing.assert_array_equal(g_out.to_numpy(), gref.values())
+    assert frob(m_out.to_numpy(), A @ B) <= 1e-13
+
+
 # ---------------------------------------------------- memory-bound workload
 
 
