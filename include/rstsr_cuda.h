@@ -524,7 +524,8 @@ typedef enum {
 /* Tuning knobs shared by the GEMM entry points. Zero-initialise for defaults. */
 typedef struct {
     int32_t precision;      /* rstsr_precision */
-    int32_t ozaki_slices;   /* 0 = choose from the operands' exponent spread */
+    int32_t ozaki_slices;   /* 0 = choose from the operands' exponent spread (8 for calls of
+                               at most 2^30 multiply-adds, without measuring it) */
     int32_t reserved[6];
 } rstsr_gemm_opts;
 

@@ -370,6 +370,12 @@ static int kt_for_stages(int slices, int bn) {
     return 16;
 }
 
+// Calls of at most this many multiply-adds skip the spread measurement and
+// run with the largest slice count (8): measured on GB300 the synchronisation
+// that brings the spread to the host costs 10-25 us, more than the extra
+// products below about 2^30 multiply-adds.
+constexpr double kNoSpreadMacs = 1073741824.0;
+
 // Slices needed for <= 1e-12 relative error given the spread (log2 of row
 // max over row mean |x|) of both operands. Dropping the levels >= L leaves an
 // error near 2^(-7L + spreadA + spreadB - 6) of the result (measured on GB300:
@@ -492,6 +498,12 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
         cudaStreamCaptureStatus cs;
         if (cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess) capturing = cs != cudaStreamCaptureStatusNone;
         if (L <= 0 && capturing) L = 7;  // no host round trip inside a graph capture
+        // up to 2^30 multiply-adds the spread's host round trip (a stream
+        // synchronisation, 10-25 us) costs more than the products of the
+        // largest slice count: take 8, which no automatic choice exceeds
+        double macs = 0;
+        for (const auto& q : probs) macs += (double)q.M * (double)q.N * (double)q.K;
+        if (L <= 0 && macs <= kNoSpreadMacs) L = 8;
         if (L <= 0) {
             // choose the slice count from the exponent spread of each side,
             // reduced on the device: one synchronisation, 8 bytes back
@@ -512,8 +524,6 @@ int split_gemm_run(rstsr_ctx* ctx, SplitMode mode, const std::vector<SplitItem>&
             float fa, fb;
             memcpy(&fa, &hsp[0], 4);
             memcpy(&fb, &hsp[1], 4);
-            double macs = 0;
-            for (const auto& q : probs) macs += (double)q.M * (double)q.N * (double)q.K;
             L = auto_levels(fa, b_items.empty() ? fa : fb, macs <= 16777216.0);
         }
         L = std::min(std::max(L, 1), 8);
