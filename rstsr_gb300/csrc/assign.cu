@@ -41,6 +41,11 @@ struct TrParams {
     FastDiv div_t0, div_tj;
     uint32_t tiles0, tilesj;
     uint32_t ntiles;
+    // transpose2_kernel: dim j folded with the batch dim that continues it in
+    // the source (source stride nj_in): column ij of the tile writes at
+    // (ij mod nj_in) * out_sj + (ij / nj_in) * out_sjo; jlog = log2(nj_in), 0 = no fold
+    int jlog;
+    int64_t out_sjo;
 };
 
 // Source contiguous along dim j, destination along dim 0: reads coalesce along
@@ -127,7 +132,9 @@ __global__ void __launch_bounds__(32 * kTileRows)
                 uint2 w;
                 w.x = tile[2 * tx][ty + r * kTileRows];
                 w.y = tile[2 * tx + 1][ty + r * kTileRows];
-                *reinterpret_cast<uint2*>(out + ob + i0 + ij * p.out_sj) = w;
+                const int64_t oj = p.jlog ? (ij & ((1 << p.jlog) - 1)) * p.out_sj + (ij >> p.jlog) * p.out_sjo
+                                          : ij * p.out_sj;
+                *reinterpret_cast<uint2*>(out + ob + i0 + oj) = w;
             }
         }
         __syncthreads();
@@ -184,6 +191,30 @@ static int launch_transpose(rstsr_ctx* ctx, const IterSpace& sp, int j, void* ou
                  (p.out_sj % 2) == 0 && (p.in_off % 2) == 0 && (p.out_off % 2) == 0 &&
                  (reinterpret_cast<uintptr_t>(in) % 8) == 0 && (reinterpret_cast<uintptr_t>(out) % 8) == 0;
     for (int i = 0; pairs && i < nb; ++i) pairs = (p.in_bs[i] % 2) == 0 && (p.out_bs[i] % 2) == 0;
+    // a contiguous source run shorter than the 64-wide tile (a power of two):
+    // fold the batch dim that continues it in the source into the tile's
+    // columns, so that the tile stays full (an F-ordered [32, ...] source
+    // otherwise left half of every tile empty)
+    if (pairs && p.nj < kTile2 && (p.nj & (p.nj - 1)) == 0) {
+        for (int i = 0; i < nb; ++i) {
+            if (p.in_bs[i] != p.nj || p.bshape[i] < 2) continue;
+            int lg = 0;
+            while ((int64_t(1) << lg) < p.nj) ++lg;
+            p.jlog = lg;
+            p.out_sjo = p.out_bs[i];
+            p.nj *= p.bshape[i];
+            nbatch /= p.bshape[i];
+            for (int k = i; k + 1 < nb; ++k) {
+                p.bshape[k] = p.bshape[k + 1];
+                p.bdiv[k] = p.bdiv[k + 1];
+                p.in_bs[k] = p.in_bs[k + 1];
+                p.out_bs[k] = p.out_bs[k + 1];
+            }
+            --nb;
+            p.nb = nb;
+            break;
+        }
+    }
     const int tile = pairs ? kTile2 : kTile;
     p.tiles0 = (uint32_t)((p.n0 + tile - 1) / tile);
     p.tilesj = (uint32_t)((p.nj + tile - 1) / tile);

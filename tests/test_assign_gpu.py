@@ -52,6 +52,24 @@ def test_permute_to_contig_transpose_paths(dev, shape, axes, dtype):
         np.testing.assert_array_equal(got, np.transpose(base, axes))
 
 
+@pytest.mark.parametrize("shape", [(16, 6, 50, 40), (32, 3, 70), (32, 64, 9, 130), (16, 2, 17, 64)])
+@pytest.mark.parametrize("dtype", [np.float32, np.int32])
+def test_transpose_folds_short_source_runs(dev, shape, dtype):
+    """F-ordered 4-byte sources whose contiguous leading extent (16 or 32) is
+    shorter than the 64-wide pair tile, copied to C order: the tile folds the
+    next source dim into its columns (partial last column tiles included)."""
+    base = rand(shape, dtype, seed=6)
+    t = rt.from_host_layout(base.ravel(order="F"), shape, OL.f_stride(shape), 0, dev)
+    np.testing.assert_array_equal(t.to_contig("C").to_numpy(), base)
+    # the same through a permuted view, and from an offset (even) start
+    perm = (1, 0) + tuple(range(2, len(shape)))
+    np.testing.assert_array_equal(t.permute_dims(perm).to_contig("C").to_numpy(), np.transpose(base, perm))
+    big = rand((shape[0] + 2,) + shape[1:], dtype, seed=7)
+    tb = rt.from_host_layout(big.ravel(order="F"), big.shape, OL.f_stride(big.shape), 0, dev)
+    v = tb.i((slice(2, None),))
+    np.testing.assert_array_equal(v.to_contig("C").to_numpy(), big[2:])
+
+
 def test_assign_same_shape_all_layout_pairs(dev):
     for ka in KINDS:
         for kc in ["c", "f", "flip"]:
