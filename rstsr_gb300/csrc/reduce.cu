@@ -282,9 +282,8 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         // OV-wide vector load per reduced element; measured on GB300 the
         // scalar form reached 22 % of DRAM bandwidth (f32 sum_axes over an
         // F-ordered tensor, 4096 outputs), latency-bound with ~20 KB in
-        // flight per SM. A CTA keeps 256 x 4 loads in flight (16 KB with
-        // 16-byte loads): aim for four CTAs per SM, each walking a long
-        // chunk (fewer partials to write and fold).
+        // flight per SM. A CTA keeps 256 x 8 vector loads in flight (32 KB)
+        // or 256 x 4 scalar ones.
         p.glog = 0;
         const int OV = es >= 16 ? 1 : (16 / (int)es >= 4 ? 4 : 16 / (int)es);
         bool cv = OV > 1 && p.k.nd > 0 && p.k.in_stride[0] == 1 && (p.k.shape[0] % OV) == 0;
@@ -296,8 +295,17 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         const int64_t opc = (int64_t)kRedThreads * p.ocol;
         const int64_t gx = (p.nout + opc - 1) / opc;
         const int64_t col_target = 4 * (int64_t)ctx->num_sms;
+        // With vector loads, split the reduced range only when the outputs
+        // alone give fewer CTAs than SMs: with one CTA per SM or more the
+        // loads in flight cover the HBM latency, and a split's partials (24
+        // bytes per output and chunk for an arg reduction) and combine pass
+        // cost more than they bring (f32 argmax over the last axis of an
+        // F-ordered [32,64,128,128]: 48.9 us in three chunks, 30.7 us
+        // unsplit). Scalar walks aim for four CTAs per SM, each walking a
+        // long chunk.
+        const int64_t split_below = p.ocol > 1 ? (int64_t)ctx->num_sms : col_target;
         int64_t nsplit = 1;
-        if (gx < col_target && p.nred > 16)
+        if (gx < split_below && p.nred > 16)
             nsplit = std::min<int64_t>((col_target + gx - 1) / gx, (p.nred + 15) / 16);
         nsplit = std::max<int64_t>(1, std::min<int64_t>(nsplit, 65535));
         int64_t chunk = (p.nred + nsplit - 1) / nsplit;

@@ -537,6 +537,10 @@ __device__ __forceinline__ A shfl_down_acc(const A& a, int delta, int width) {
 // OV-wide loads and OV accumulators take more registers)
 constexpr int kRedUnroll = 8;
 constexpr int kRedUnrollCol = 4;
+// the column walk with OV-wide vector loads: eight in flight (45-48 registers,
+// five CTAs per SM); measured on GB300 against four and sixteen on the
+// F-ordered [32,64,128,128] sums and argmax
+constexpr int kRedUnrollColVec = 8;
 
 // ---------------------------------------------------------------- kernels
 
@@ -723,7 +727,7 @@ __device__ __forceinline__ typename RedLocal<T, KIND>::Local red_rows(const RedP
 // dim 0 is contiguous and one OV-wide vector load per reduced element serves
 // them all) and walks the reduced elements of its chunk in order, the
 // (row, column) position advancing by one.
-template <typename T, int KIND, int OV, bool MONO>
+template <typename T, int KIND, int OV, bool MONO, int UC>
 __device__ __forceinline__ void red_cols(const RedParams& p, const T* __restrict__ in, int64_t base,
                                          typename RedLocal<T, KIND>::Local (&acc)[OV]) {
     using R = RedLocal<T, KIND>;
@@ -737,11 +741,11 @@ __device__ __forceinline__ void red_cols(const RedParams& p, const T* __restrict
     uint32_t c = (uint32_t)rb - row * n0;
     uint32_t lrow;
     int64_t roff = red_row_offset(p.r, row, &lrow);
-    for (int64_t r = rb; r < re; r += kRedUnrollCol) {
-        RVec<T, OV> v[kRedUnrollCol];
-        uint32_t li[kRedUnrollCol];
+    for (int64_t r = rb; r < re; r += UC) {
+        RVec<T, OV> v[UC];
+        uint32_t li[UC];
 #pragma unroll
-        for (int u = 0; u < kRedUnrollCol; ++u) {
+        for (int u = 0; u < UC; ++u) {
             if (r + u < re) {
                 li[u] = MONO ? (uint32_t)(r + u) : lrow + c * l0;
                 v[u] = *reinterpret_cast<const RVec<T, OV>*>(in + base + roff + (int64_t)c * s0);
@@ -753,7 +757,7 @@ __device__ __forceinline__ void red_cols(const RedParams& p, const T* __restrict
             }
         }
 #pragma unroll
-        for (int u = 0; u < kRedUnrollCol; ++u)
+        for (int u = 0; u < UC; ++u)
             if (r + u < re) {
 #pragma unroll
                 for (int j = 0; j < OV; ++j) {
@@ -805,7 +809,7 @@ __device__ __forceinline__ void red_store(const RedParams& p, int64_t o, const t
 }
 
 // Column regime: one thread per output, or per OV neighbouring outputs.
-template <typename T, int KIND, int OV, bool MONO>
+template <typename T, int KIND, int OV, bool MONO, int UC = kRedUnrollCol>
 __global__ void __launch_bounds__(kRedThreads) reduce_col_kernel(const RedParams p) {
     using R = RedLocal<T, KIND>;
     using Acc = typename R::Acc;
@@ -816,7 +820,7 @@ __global__ void __launch_bounds__(kRedThreads) reduce_col_kernel(const RedParams
     typename R::Local acc[OV];
 #pragma unroll
     for (int j = 0; j < OV; ++j) acc[j] = R::linit();
-    red_cols<T, KIND, OV, MONO>(p, in, base, acc);
+    red_cols<T, KIND, OV, MONO, UC>(p, in, base, acc);
 #pragma unroll
     for (int j = 0; j < OV; ++j) {
         Acc a = R::to_acc(acc[j]);
@@ -896,9 +900,9 @@ cudaError_t launch_reduce_pass(const RedParams& p, dim3 grid, cudaStream_t strea
         }
     } else if (OV > 1 && p.ocol > 1) {
         if (mono)
-            reduce_col_kernel<T, KIND, OV, kArg><<<grid, kRedThreads, 0, stream>>>(p);
+            reduce_col_kernel<T, KIND, OV, kArg, kRedUnrollColVec><<<grid, kRedThreads, 0, stream>>>(p);
         else
-            reduce_col_kernel<T, KIND, OV, false><<<grid, kRedThreads, 0, stream>>>(p);
+            reduce_col_kernel<T, KIND, OV, false, kRedUnrollColVec><<<grid, kRedThreads, 0, stream>>>(p);
     } else {
         if (mono)
             reduce_col_kernel<T, KIND, 1, kArg><<<grid, kRedThreads, 0, stream>>>(p);
