@@ -360,7 +360,8 @@ __global__ void __launch_bounds__(256) split_kernel(const SegPair segs, int pitc
 
 // K tile width: the widest of 64 / 32 / 16 whose pipeline stage (every slice
 // of a 128-row A tile and a BN-row B tile) leaves room for four stages, so
-// that TMA latency stays hidden behind the products of the other stages.
+// that the bulk-copy latency stays hidden behind the products of the other
+// stages.
 static int kt_for_stages(int slices, int bn) {
     const size_t budget = kTcSmemMax - 1024 - kTcSmemTail;
     for (int kt : {64, 32}) {

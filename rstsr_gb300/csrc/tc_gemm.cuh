@@ -1,4 +1,4 @@
-// Multi-product tensor-core GEMM for sm_103a (tcgen05 + TMA + TMEM).
+// Multi-product tensor-core GEMM for sm_103a (tcgen05 + bulk copies + TMEM).
 //
 // Work unit: a 128 x 64 output tile and one K chunk of it. The operands are
 // stacks of bf16 "slices" written by the split kernel directly in the tensor
@@ -29,8 +29,8 @@
 //   * the Ozaki split for f64 (L integer slices, L level slots),
 //   * the three-term bf16 split for f32 (hi/mid/lo, three level slots),
 // for a single problem or for a list of problems (batched and grouped
-// matmul) whose slices share one pair of TMA maps, read from a device tile
-// list {problem, tile row, tile column}.
+// matmul) whose slices share one pair of operand stacks, read from a device
+// tile list {problem, tile row, tile column}.
 //
 // Persistent: one CTA per SM walks tiles blockIdx.x, + gridDim.x, ... Roles
 // (576 threads): warp 0 streams bulk copies through a ring of stages, warp 1

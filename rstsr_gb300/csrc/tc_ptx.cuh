@@ -1,5 +1,5 @@
 // Inline-PTX building blocks of the Blackwell (sm_103a) tensor-core path:
-// mbarriers, TMA tensor loads, tcgen05 (TMEM allocation, MMA, commit, loads)
+// mbarriers, bulk copies (cp.async.bulk), tcgen05 (TMEM allocation, MMA, commit, loads)
 // and the shared-memory / instruction descriptors of tcgen05.mma.
 //
 // Every wait in this file is bounded: after kWaitLimitCycles SM cycles
@@ -7,7 +7,6 @@
 // raise the kernel's error flag and unwind instead of hanging the GPU.
 #pragma once
 
-#include <cuda.h>
 #include <cstdint>
 
 namespace rstsr {
@@ -91,16 +90,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     }
 }
 
-// ------------------------------------------------------------------ TMA
-
-__device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* map, uint64_t* bar, int32_t x,
-                                            int32_t y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
-            smem_u32(smem_dst)),
-        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
-        : "memory");
-}
+// ------------------------------------------------------------ bulk copy
 
 // Contiguous copy global -> shared of `bytes` (multiple of 16, both addresses
 // 16-byte aligned), completing as transaction bytes on `bar`.
@@ -110,10 +100,6 @@ __device__ __forceinline__ void bulk_load(void* smem_dst, const void* gsrc, uint
             smem_u32(smem_dst)),
         "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
         : "memory");
-}
-
-__device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
-    asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
 }
 
 // --------------------------------------------------------------- tcgen05
@@ -154,22 +140,8 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                  : "memory");
 }
 
-// 32 lanes x 32 consecutive 32-bit columns: thread i of the warp receives
-// TMEM lane (quadrant base + i), columns [col, col + 32).
-__device__ __forceinline__ void tmem_ld_32x32b_x32(uint32_t taddr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr)
-        : "memory");
-}
-
-// The same for 16 consecutive columns.
+// 32 lanes x 16 consecutive 32-bit columns: thread i of the warp receives
+// TMEM lane (quadrant base + i), columns [col, col + 16).
 __device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, uint32_t* r) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
@@ -196,29 +168,12 @@ __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.
 
 // ------------------------------------------------------------ descriptors
 
-// Shared-memory matrix descriptor of tcgen05.mma for a K-major operand tile
-// stored the way a TMA load with the matching swizzle writes it: rows of
-// `row_bytes` (32, 64 or 128 bytes), 8-row swizzle atoms of 8 * row_bytes
-// bytes stacked along M/N (stride byte offset), leading byte offset unused.
-// Fields: start address >> 4 (bits 0-13), LBO >> 4 (16-29), SBO >> 4 (32-45),
-// fixed version 1 (46-47), base offset 0 (49-51), swizzle mode (61-63:
-// 2 = 128-byte, 4 = 64-byte, 6 = 32-byte).
-__device__ __forceinline__ uint64_t smem_desc_kmajor(uint32_t saddr, uint32_t row_bytes) {
-    const uint64_t sbo = (uint64_t)(8 * row_bytes) >> 4;
-    const uint64_t mode = row_bytes == 128 ? 2 : row_bytes == 64 ? 4 : 6;
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-    d |= (uint64_t)1 << 16;  // LBO (unused for swizzled K-major)
-    d |= (sbo & 0x3FFF) << 32;
-    d |= (uint64_t)1 << 46;  // descriptor version
-    d |= mode << 61;
-    return d;
-}
-
-// The same for the layout without swizzle: the operand is made of "core
-// matrices" of 8 rows x 16 bytes (128 contiguous bytes); LBO is the byte step
-// between core matrices along K, SBO along M/N; swizzle mode 0. Returns the
-// descriptor without its start address (bits 0-13).
+// Shared-memory matrix descriptor of tcgen05.mma for a K-major operand
+// without swizzle: the operand is made of "core matrices" of 8 rows x 16
+// bytes (128 contiguous bytes); LBO is the byte step between core matrices
+// along K, SBO along M/N. Fields: start address >> 4 (bits 0-13), LBO >> 4
+// (16-29), SBO >> 4 (32-45), fixed version 1 (46-47), base offset 0 (49-51),
+// swizzle mode 0 (61-63). Returns the descriptor without its start address.
 __host__ __device__ constexpr uint64_t smem_desc_noswizzle(uint32_t lbo, uint32_t sbo) {
     return ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
 }
