@@ -421,7 +421,7 @@ def gemm_summary(g, small):
     out = {}
     for name in ("c4_split_f32_8192", "c4_split_f32_tall"):
         e = g[name]
-        out[name] = {"tflops": e["tflops"], "rel_err": float(f"{e['rel_err_vs_fp64']:.3g}"),
+        out[name] = {"tflops": e["tflops"], "rel_err": float(f"{e['rel_err_vs_fp64']:.3g}"), "tuned": True,
                      "sgemm_tflops": e["cublas_sgemm_tflops"],
                      "bf16x9_tflops": e.get("cublas_emulated_bf16x9", {}).get("tflops")}
     gr, bc, ch = g["c5_grouped_f64_512"], g["c5_broadcast_batch_f64"], g["c5_graph_chain_f64"]
@@ -627,6 +627,8 @@ def run_gemm_section(dev, stream):
         b = (rng.uniform(-1, 1, (k, n)) * 2.0 ** rng.uniform(-8, 8, (k, n))).astype(np.float32)
         ta, tb2 = rt.asarray(a, dev), rt.asarray(b, dev)
         c = rt.empty((m, n), np.float32, dev)
+        # tile configuration from the project's autotuner for this shape class
+        code = rt.autotune_gemm(dev, np.float32, m, n, k)
         sec = _time_events(stream, lambda: rt.matmul_into(c, ta, tb2), 3)
         fa, fb = torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda()
         ref = fa.double() @ fb.double()
@@ -637,6 +639,7 @@ def run_gemm_section(dev, stream):
         nr = torch.linalg.norm(ref)
         out[name] = {
             "shape": f"{m}x{n}x{k}", "tflops": round(2.0 * m * n * k / sec / 1e12, 2), "ms": round(sec * 1e3, 3),
+            "tuned_config": {"k_tile": code & 255, "group": code >> 8},
             "rel_err_vs_fp64": (torch.linalg.norm(got - ref) / nr).item(),
             "cublas_sgemm_tflops": round(2.0 * m * n * k / sec_s / 1e12, 2),
             "cublas_sgemm_rel_err_vs_fp64": (torch.linalg.norm(sref - ref) / nr).item(),
@@ -1221,6 +1224,39 @@ def run_per_case_only(args):
     return {"section": "per_case", "peak_gbs": peak, "cases": cases, "torch": torch_res}
 
 
+def run_c4_only(args):
+    """Only the f32 three-term split GEMM (profiling): A [n, n] and B [n, n]
+    uniform(-1, 1) scaled by 2^U(-8, 8), seed 0, C = A B in f32; with
+    --c4-tune the project's autotuner picks the tile configuration first.
+    CUDA events over --steps calls after --warmup."""
+    import torch
+
+    import rstsr_gb300 as rt
+
+    dev = rt.DeviceCuda(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    dev.set_stream(stream.cuda_stream)
+    n = args.c4_n
+    rng = np.random.default_rng(0)
+    a = (rng.uniform(-1, 1, (n, n)) * 2.0 ** rng.uniform(-8, 8, (n, n))).astype(np.float32)
+    b = (rng.uniform(-1, 1, (n, n)) * 2.0 ** rng.uniform(-8, 8, (n, n))).astype(np.float32)
+    ta, tb = rt.asarray(a, dev), rt.asarray(b, dev)
+    c = rt.empty((n, n), np.float32, dev)
+    res = {"section": "c4", "n": n}
+    if args.c4_tune:
+        code = rt.autotune_gemm(dev, np.float32, n, n, n)
+        res["tuned_config"] = {"k_tile": code & 255, "group": code >> 8}
+    for _ in range(max(args.warmup - 1, 0)):
+        rt.matmul_into(c, ta, tb)
+    sec = _time_events(stream, lambda: rt.matmul_into(c, ta, tb), max(args.steps, 1))
+    res.update({"ms": round(sec * 1e3, 3), "tflops": round(2.0 * n ** 3 / sec / 1e12, 2)})
+    ref = torch.from_numpy(a).cuda().double() @ torch.from_numpy(b).cuda().double()
+    got = torch.as_tensor(c.to_numpy()).cuda().double()
+    res["rel_err_vs_fp64"] = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
+    return res
+
+
 def run_batched_only(args):
     """Only the batched / grouped GEMM section (profiling)."""
     import torch
@@ -1535,12 +1571,14 @@ def main():
     ap.add_argument("--rate-n", type=int, default=8192, help="matrix order for --only rates")
     ap.add_argument("--trsm-n", type=int, default=4096, help="order (and right-hand sides) for --only trsm")
     ap.add_argument("--only", default="",
-                    choices=["", "c3", "tri_index", "contraction", "rates", "batched", "trsm", "per_case"],
+                    choices=["", "c3", "c4", "tri_index", "contraction", "rates", "batched", "trsm", "per_case"],
                     help="c3: only the Ozaki contraction; tri_index: only pack/unpack_tri and index_select; "
                          "contraction: only einsum / vecdot; rates: INT8 / BF16 / FP64 tensor rates; batched: only C5; "
-                         "trsm: only TRSM; per_case: each operation of the strided workload per (dtype, layout), "
+                         "c4: only the f32 split GEMM (--c4-n, --c4-tune); trsm: only TRSM; per_case: each operation of the strided workload per (dtype, layout), "
                          "with torch's reductions on the same bytes")
     ap.add_argument("--ein-p", type=int, default=1000, help="P of the 3-index transform for --only contraction")
+    ap.add_argument("--c4-n", type=int, default=8192, help="order of the f32 product for --only c4")
+    ap.add_argument("--c4-tune", action="store_true", help="autotune the tile configuration first (--only c4)")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
     ap.add_argument("--tri-batch", type=int, default=32, help="matrices for --only tri_index")
@@ -1557,6 +1595,8 @@ def main():
         res = run_trsm_only(args)
     elif args.only == "per_case":
         res = run_per_case_only(args)
+    elif args.only == "c4":
+        res = run_c4_only(args)
     elif args.only == "tri_index":
         res = run_tri_index_only(args)
     elif args.only == "contraction":
