@@ -36,6 +36,23 @@ def test_ozaki_f64_matmul(dev, m, n, k):
     assert rt.lib().rstsr_cuda_last_ozaki_slices() >= 4
 
 
+@pytest.mark.parametrize("m,n,k,want", [(512, 512, 512, 8), (1024, 1024, 1024, 8), (1024, 1024, 1025, 0)])
+def test_ozaki_slice_count_rule(dev, m, n, k, want):
+    """Calls of at most 2^30 multiply-adds take 8 slices without measuring the
+    exponent spread; larger ones choose from the spread (4-8). Rows scaled by
+    2^U(-30, 30) and a decaying K profile keep the spread wide."""
+    rng = np.random.default_rng(m + k)
+    a = rng.standard_normal((m, k)) * 2.0 ** rng.uniform(-30, 30, (m, 1)) * np.exp(-0.004 * np.arange(k))
+    b = rng.standard_normal((k, n)) * 2.0 ** rng.uniform(-30, 30, (1, n))
+    c = (rt.asarray(a, dev) % rt.asarray(b, dev)).to_numpy()
+    got = rt.lib().rstsr_cuda_last_ozaki_slices()
+    if want:
+        assert got == want
+    else:
+        assert 4 <= got <= 8
+    assert rel_err(c, ref64(a, b)) <= F64_TOL
+
+
 def test_ozaki_exponent_spread_and_signs(dev):
     rng = np.random.default_rng(1)
     m, n, k = 150, 140, 300
