@@ -220,14 +220,19 @@ int plan_reduce(rstsr_ctx* ctx, int op, rstsr_dtype t_in, const void* a, const L
         p.chunk = 1;
     } else if (rin <= kin) {
         // row regime. Group size from the vector loads per output (nvec):
-        // short runs give each lane about 8 of them (one round of loads in
-        // flight; a warp's accesses stay whole 64-128-byte pieces of each
-        // run), long runs about 32 (four rounds: a CTA that issues only one
-        // round spends most of its life waiting for it); G <= 256
+        // short runs give each lane about 16 of them, long runs about 32
+        // (a CTA that issues only one round of loads spends most of its life
+        // waiting for it); 8-byte elements twice as many (their rounds are
+        // four loads, and their folds are integer-pipe work that the longer
+        // walks overlap with the loads). G <= 256. Measured on GB300 over the
+        // [32,64,128,128] workload against 8 / 32 vectors a lane for every
+        // type: f64 argmax over the last axis 0.57 -> 0.67 of HBM (C and
+        // permuted), f64 sums over axes (1, 3) 0.59 -> 0.64, the step-2
+        // sliced argmax 0.35 -> 0.37 (4-byte) and 0.40 -> 0.44 (f64).
         const bool s2_shape = VEC >= 4 && p.r.stride[0] == 2 && (p.r.shape[0] % (VEC / 2)) == 0;
         const int64_t W = p.r.stride[0] == 1 && (p.r.shape[0] % VEC) == 0 ? VEC : s2_shape ? VEC / 2 : 1;
         const int64_t nvec = (p.nred + W - 1) / W;
-        const int64_t per_lane = nvec <= 1024 ? 8 : 32;
+        const int64_t per_lane = (nvec <= 1024 ? 16 : 32) * (es >= 8 ? 2 : 1);
         int G = 1, glog = 0;
         while (G < 256 && (int64_t)G * 2 * per_lane <= nvec) {
             G <<= 1;
