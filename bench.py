@@ -1225,8 +1225,9 @@ def run_per_case_only(args):
 
 
 def run_c4_only(args):
-    """Only the f32 three-term split GEMM (profiling): A [n, n] and B [n, n]
-    uniform(-1, 1) scaled by 2^U(-8, 8), seed 0, C = A B in f32; with
+    """Only the f32 three-term split GEMM (profiling): A [m, k] and B [k, n]
+    (--c4-shape, else m = n = k = --c4-n) uniform(-1, 1) scaled by
+    2^U(-8, 8), seed 0, C = A B in f32; with
     --c4-tune the project's autotuner picks the tile configuration first.
     CUDA events over --steps calls after --warmup."""
     import torch
@@ -1237,20 +1238,20 @@ def run_c4_only(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     dev.set_stream(stream.cuda_stream)
-    n = args.c4_n
+    m, n, k = (int(x) for x in args.c4_shape.split(",")) if args.c4_shape else (args.c4_n,) * 3
     rng = np.random.default_rng(0)
-    a = (rng.uniform(-1, 1, (n, n)) * 2.0 ** rng.uniform(-8, 8, (n, n))).astype(np.float32)
-    b = (rng.uniform(-1, 1, (n, n)) * 2.0 ** rng.uniform(-8, 8, (n, n))).astype(np.float32)
+    a = (rng.uniform(-1, 1, (m, k)) * 2.0 ** rng.uniform(-8, 8, (m, k))).astype(np.float32)
+    b = (rng.uniform(-1, 1, (k, n)) * 2.0 ** rng.uniform(-8, 8, (k, n))).astype(np.float32)
     ta, tb = rt.asarray(a, dev), rt.asarray(b, dev)
-    c = rt.empty((n, n), np.float32, dev)
-    res = {"section": "c4", "n": n}
+    c = rt.empty((m, n), np.float32, dev)
+    res = {"section": "c4", "shape": [m, n, k]}
     if args.c4_tune:
-        code = rt.autotune_gemm(dev, np.float32, n, n, n)
+        code = rt.autotune_gemm(dev, np.float32, m, n, k)
         res["tuned_config"] = {"k_tile": code & 255, "group": code >> 8}
     for _ in range(max(args.warmup - 1, 0)):
         rt.matmul_into(c, ta, tb)
     sec = _time_events(stream, lambda: rt.matmul_into(c, ta, tb), max(args.steps, 1))
-    res.update({"ms": round(sec * 1e3, 3), "tflops": round(2.0 * n ** 3 / sec / 1e12, 2)})
+    res.update({"ms": round(sec * 1e3, 3), "tflops": round(2.0 * m * n * k / sec / 1e12, 2)})
     ref = torch.from_numpy(a).cuda().double() @ torch.from_numpy(b).cuda().double()
     got = torch.as_tensor(c.to_numpy()).cuda().double()
     res["rel_err_vs_fp64"] = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
@@ -1578,6 +1579,7 @@ def main():
                          "with torch's reductions on the same bytes")
     ap.add_argument("--ein-p", type=int, default=1000, help="P of the 3-index transform for --only contraction")
     ap.add_argument("--c4-n", type=int, default=8192, help="order of the f32 product for --only c4")
+    ap.add_argument("--c4-shape", default="", help="M,N,K of the f32 product for --only c4 (overrides --c4-n)")
     ap.add_argument("--c4-tune", action="store_true", help="autotune the tile configuration first (--only c4)")
     ap.add_argument("--c3-cols", type=int, default=15000, help="columns of Bm for --only c3")
     ap.add_argument("--tri-n", type=int, default=2048, help="matrix order for --only tri_index")
